@@ -1,0 +1,451 @@
+// extern "C" entry points of include/bg.h: argument checks, host <-> device staging in the
+// wire layout of bend2/FORMAT.md, and the mapping of exceptions to BG_E_* statuses.
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "ec.cuh"
+#include "host_ff.hpp"
+#include "msm.h"
+#include "ntt.h"
+#include "prims.h"
+#include "prove.h"
+
+namespace bg {
+std::atomic<uint64_t> g_launches{0};
+void synth_square_chain(Ctx& c, uint32_t log2n, uint64_t seed, const std::string& dir);
+}
+
+struct bg_ctx {
+  bg::Ctx c;
+};
+struct bg_pk {
+  bg::PkDev* pk;
+  bg_ctx* owner;
+};
+
+using namespace bg;
+
+namespace {
+
+thread_local std::string g_err_noctx;
+
+template <class Fn>
+int guard(bg_ctx* ctx, Fn&& fn) {
+  try {
+    fn();
+    if (ctx) ctx->c.last_error.clear();
+    return BG_OK;
+  } catch (const Error& e) {
+    if (ctx) ctx->c.last_error = e.what();
+    else g_err_noctx = e.what();
+    if (ctx && e.status == BG_E_DEVICE) cudaGetLastError();
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->c.last_error = "host allocation failed";
+    return BG_E_OOM;
+  } catch (const std::exception& e) {
+    if (ctx) ctx->c.last_error = e.what();
+    return BG_E_DEVICE;
+  }
+}
+
+void require(bool ok, const char* msg) {
+  if (!ok) throw Error(BG_E_ARG, msg);
+}
+
+// copy n wire elements (16 words each) from the host and repack them on the device
+uint32_t* stage_in(Ctx& c, const std::string& name, const uint32_t* host16, size_t n_elems) {
+  uint32_t* wire = c.ws.get_t<uint32_t>(name + ".wire", n_elems * 16);
+  uint32_t* packed = c.ws.get_t<uint32_t>(name, n_elems * 8);
+  BG_CUDA(cudaMemcpyAsync(wire, host16, n_elems * 64, cudaMemcpyHostToDevice, c.stream));
+  wire_to_packed(c.stream, wire, packed, n_elems, c.d_status);
+  return packed;
+}
+
+void stage_out(Ctx& c, const std::string& name, const uint32_t* d_packed, uint32_t* host16, size_t n_elems) {
+  uint32_t* wire = c.ws.get_t<uint32_t>(name + ".wire_out", n_elems * 16);
+  packed_to_wire(c.stream, d_packed, wire, n_elems);
+  BG_CUDA(cudaMemcpyAsync(host16, wire, n_elems * 64, cudaMemcpyDeviceToHost, c.stream));
+}
+
+// affine packed result -> Jacobian wire words (x, y, z) with z = 1, infinity = (0, 1, 0)
+template <class H>
+void affine_to_jacobian_wire(const uint32_t* aff32, uint32_t* jac16) {
+  constexpr int W = H::WORDS;  // packed words per field element
+  bool inf = true;
+  for (int i = 0; i < 2 * W; i++) inf &= aff32[i] == 0;
+  uint32_t packed[3 * W];
+  memset(packed, 0, sizeof(packed));
+  const bgh::Fe one = bgh::fe_one(bgh::FQ);
+  if (inf) {
+    bgh::fe_to_words32(packed + W, one);  // y = 1 (c0 of Fq2), x = z = 0
+  } else {
+    memcpy(packed, aff32, sizeof(uint32_t) * 2 * W);
+    bgh::fe_to_words32(packed + 2 * W, one);
+  }
+  for (int i = 0; i < 3 * W; i++) {
+    jac16[2 * i] = packed[i] & 0xffffu;
+    jac16[2 * i + 1] = packed[i] >> 16;
+  }
+}
+
+template <class F, class H>
+void msm_host(Ctx& c, const uint32_t* points16, const uint32_t* scalars16, size_t n, uint32_t* out_jac16) {
+  constexpr int PW = 2 * H::WORDS;  // packed words per affine point
+  uint32_t aff[2 * 16];
+  if (n == 0) {
+    memset(aff, 0, sizeof(aff));
+  } else {
+    const uint32_t* pts = stage_in(c, "api.msm_pts", points16, n * (PW / 8));
+    // scalars are canonical: repack without a Montgomery conversion
+    const uint32_t* sc = stage_in(c, "api.msm_sc", scalars16, n);
+    MsmPlan plan;
+    msm_launch<F>(c, c.stream, "api.msm", pts, sc, n, plan);
+    msm_fetch<F>(c.stream, plan);
+    BG_CUDA(cudaStreamSynchronize(c.stream));
+    check_status(c, c.stream);
+    msm_finish<F>(plan, aff);
+  }
+  affine_to_jacobian_wire<H>(aff, out_jac16);
+}
+
+template <class F>
+void msm_dev(Ctx& c, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32) {
+  constexpr int PW = 2 * FieldWords<F>::value;
+  if (n == 0) {
+    memset(out_aff32, 0, PW * 4);
+    return;
+  }
+  MsmPlan plan;
+  msm_launch<F>(c, c.stream, "api.msm", d_points, d_scalars, n, plan);
+  msm_fetch<F>(c.stream, plan);
+  BG_CUDA(cudaStreamSynchronize(c.stream));
+  check_status(c, c.stream);
+  msm_finish<F>(plan, out_aff32);
+}
+
+bool read_file(const std::string& path, std::vector<char>& out) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return false;
+  fseek(f, 0, SEEK_END);
+  long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  out.resize(sz > 0 ? (size_t)sz : 0);
+  size_t got = sz > 0 ? fread(out.data(), 1, (size_t)sz, f) : 0;
+  fclose(f);
+  return got == out.size();
+}
+
+}  // namespace
+
+extern "C" {
+
+int bg_ctx_create(int device, bg_ctx** out) {
+  if (!out) return BG_E_ARG;
+  *out = nullptr;
+  bg_ctx* ctx = new bg_ctx();
+  int st = guard(nullptr, [&] {
+    int ndev = 0;
+    BG_CUDA(cudaGetDeviceCount(&ndev));
+    require(device >= 0 && device < ndev, "bg_ctx_create: no such CUDA device");
+    BG_CUDA(cudaSetDevice(device));
+    ctx->c.device = device;
+    BG_CUDA(cudaDeviceGetAttribute(&ctx->c.sm_count, cudaDevAttrMultiProcessorCount, device));
+    BG_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
+    for (int i = 0; i < kStreams; i++) {
+      BG_CUDA(cudaStreamCreateWithFlags(&ctx->c.side[i], cudaStreamNonBlocking));
+      BG_CUDA(cudaEventCreateWithFlags(&ctx->c.ev_join[i], cudaEventDisableTiming));
+    }
+    BG_CUDA(cudaEventCreateWithFlags(&ctx->c.ev_fork, cudaEventDisableTiming));
+    ctx->c.d_status = ctx->c.ws.get_t<uint32_t>("status", 1);
+    BG_CUDA(cudaMemsetAsync(ctx->c.d_status, 0, 4, ctx->c.stream));
+    BG_CUDA(cudaStreamSynchronize(ctx->c.stream));
+  });
+  if (st != BG_OK) {
+    delete ctx;
+    return st;
+  }
+  *out = ctx;
+  return BG_OK;
+}
+
+void bg_ctx_destroy(bg_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->c.device);
+  cudaStreamSynchronize(ctx->c.stream);
+  for (int i = 0; i < kStreams; i++) {
+    if (ctx->c.side[i]) {
+      cudaStreamSynchronize(ctx->c.side[i]);
+      cudaStreamDestroy(ctx->c.side[i]);
+    }
+    if (ctx->c.ev_join[i]) cudaEventDestroy(ctx->c.ev_join[i]);
+  }
+  if (ctx->c.ev_fork) cudaEventDestroy(ctx->c.ev_fork);
+  ctx->c.ws.clear();
+  if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+}
+
+const char* bg_strerror(int status) {
+  switch (status) {
+    case BG_OK: return "ok";
+    case BG_E_ARG: return "invalid argument";
+    case BG_E_OOM: return "out of memory";
+    case BG_E_FORMAT: return "input does not match bend2/FORMAT.md";
+    case BG_E_TIMEOUT: return "device wait timed out";
+    case BG_E_DEVICE: return "CUDA error";
+    case BG_E_IO: return "file read error";
+    default: return "unknown status";
+  }
+}
+
+const char* bg_last_error(const bg_ctx* ctx) { return ctx ? ctx->c.last_error.c_str() : g_err_noctx.c_str(); }
+
+void* bg_ctx_stream(bg_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
+
+uint64_t bg_ctx_launches(const bg_ctx*) { return g_launches.load(); }
+
+int bg_host_alloc(size_t bytes, void** out) {
+  if (!out) return BG_E_ARG;
+  cudaError_t e = cudaMallocHost(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return BG_E_OOM;
+  }
+  return BG_OK;
+}
+
+void bg_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+int bg_msm_window_bits(size_t n) { return msm_pick_c(n); }
+
+int bg_msm_g1(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, size_t n, uint32_t* out_jac16) {
+  if (!ctx || !out_jac16 || (n && (!points16 || !scalars16))) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    msm_host<Fq, bgh::FqOps>(ctx->c, points16, scalars16, n, out_jac16);
+  });
+}
+
+int bg_msm_g2(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, size_t n, uint32_t* out_jac16) {
+  if (!ctx || !out_jac16 || (n && (!points16 || !scalars16))) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    msm_host<Fq2, bgh::Fq2Ops>(ctx->c, points16, scalars16, n, out_jac16);
+  });
+}
+
+int bg_msm_g1_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32) {
+  if (!ctx || !out_aff32 || (n && (!d_points || !d_scalars))) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    msm_dev<Fq>(ctx->c, d_points, d_scalars, n, out_aff32);
+  });
+}
+
+int bg_msm_g2_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32) {
+  if (!ctx || !out_aff32 || (n && (!d_points || !d_scalars))) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    msm_dev<Fq2>(ctx->c, d_points, d_scalars, n, out_aff32);
+  });
+}
+
+int bg_qap_h(bg_ctx* ctx, const uint32_t* a16, const uint32_t* b16, const uint32_t* c16, uint32_t log2d,
+             uint32_t* h16) {
+  if (!ctx || !a16 || !b16 || !c16 || !h16 || log2d > 27) return BG_E_ARG;
+  return guard(ctx, [&] {
+    Ctx& c = ctx->c;
+    cudaSetDevice(c.device);
+    const size_t d = size_t(1) << log2d;
+    uint32_t* a = stage_in(c, "api.qa", a16, d);
+    uint32_t* b = stage_in(c, "api.qb", b16, d);
+    uint32_t* cc = stage_in(c, "api.qc", c16, d);
+    uint32_t* h = c.ws.get_t<uint32_t>("api.qh", d * 8);
+    if (log2d == 0) {
+      // d = 1: h = (a b - c) / (g - 1) on the one-point coset; handled by the general path
+    }
+    qap_h_run(c, c.stream, a, b, cc, h, (int)log2d);
+    stage_out(c, "api.qh", h, h16, d);
+    BG_CUDA(cudaStreamSynchronize(c.stream));
+    check_status(c, c.stream);
+  });
+}
+
+int bg_ntt(bg_ctx* ctx, uint32_t* data16, uint32_t log2n, int mode) {
+  if (!ctx || !data16 || log2n > 27 || mode < 0 || mode > 3) return BG_E_ARG;
+  return guard(ctx, [&] {
+    Ctx& c = ctx->c;
+    cudaSetDevice(c.device);
+    const size_t n = size_t(1) << log2n;
+    uint32_t* d = stage_in(c, "api.ntt", data16, n);
+    ntt_run(c, c.stream, d, (int)log2n, mode);
+    stage_out(c, "api.ntt", d, data16, n);
+    BG_CUDA(cudaStreamSynchronize(c.stream));
+    check_status(c, c.stream);
+  });
+}
+
+int bg_ntt_dev(bg_ctx* ctx, uint32_t* d_data, uint32_t log2n, int mode) {
+  if (!ctx || !d_data || log2n > 27 || mode < 0 || mode > 3) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    ntt_run(ctx->c, ctx->c.stream, d_data, (int)log2n, mode);
+  });
+}
+
+int bg_repack_to_packed_dev(bg_ctx* ctx, const uint32_t* d_wire, uint32_t* d_packed, size_t n) {
+  if (!ctx || (n && (!d_wire || !d_packed))) return BG_E_ARG;
+  return guard(ctx, [&] { wire_to_packed(ctx->c.stream, d_wire, d_packed, n, ctx->c.d_status); });
+}
+
+int bg_repack_to_wire_dev(bg_ctx* ctx, const uint32_t* d_packed, uint32_t* d_wire, size_t n) {
+  if (!ctx || (n && (!d_wire || !d_packed))) return BG_E_ARG;
+  return guard(ctx, [&] { packed_to_wire(ctx->c.stream, d_packed, d_wire, n); });
+}
+
+int bg_field_op(bg_ctx* ctx, int field, int op, const uint32_t* a16, const uint32_t* b16, uint32_t* out16,
+                size_t n) {
+  const bool binary = op == BG_FOP_ADD || op == BG_FOP_SUB || op == BG_FOP_MUL;
+  if (!ctx || (field != BG_FIELD_FR && field != BG_FIELD_FQ) || op < 0 || op > BG_FOP_FROM_MONT) return BG_E_ARG;
+  if (n && (!a16 || !out16 || (binary && !b16))) return BG_E_ARG;
+  return guard(ctx, [&] {
+    Ctx& c = ctx->c;
+    cudaSetDevice(c.device);
+    if (n == 0) return;
+    uint32_t* a = stage_in(c, "api.fa", a16, n);
+    uint32_t* b = binary ? stage_in(c, "api.fb", b16, n) : nullptr;
+    uint32_t* o = c.ws.get_t<uint32_t>("api.fo", n * 8);
+    field_op(c.stream, field, op, a, b, o, n);
+    stage_out(c, "api.fo", o, out16, n);
+    BG_CUDA(cudaStreamSynchronize(c.stream));
+    check_status(c, c.stream);
+  });
+}
+
+int bg_curve_op(bg_ctx* ctx, int curve, int op, const uint32_t* p16, const uint32_t* q16, const uint32_t* k16,
+                uint32_t* out16, size_t n) {
+  if (!ctx || (curve != BG_CURVE_G1 && curve != BG_CURVE_G2) || op < 0 || op > BG_COP_MUL) return BG_E_ARG;
+  if (n && (!p16 || !out16 || (op == BG_COP_ADD && !q16) || (op == BG_COP_MUL && !k16))) return BG_E_ARG;
+  return guard(ctx, [&] {
+    Ctx& c = ctx->c;
+    cudaSetDevice(c.device);
+    if (n == 0) return;
+    const size_t fe = curve == BG_CURVE_G1 ? 2 : 4;  // field elements per affine point
+    uint32_t* p = stage_in(c, "api.cp", p16, n * fe);
+    uint32_t* q = op == BG_COP_ADD ? stage_in(c, "api.cq", q16, n * fe) : nullptr;
+    uint32_t* k = op == BG_COP_MUL ? stage_in(c, "api.ck", k16, n) : nullptr;
+    uint32_t* o = c.ws.get_t<uint32_t>("api.co", n * fe * 8);
+    curve_op(c.stream, curve, op, p, q, k, o, n);
+    stage_out(c, "api.co", o, out16, n * fe);
+    BG_CUDA(cudaStreamSynchronize(c.stream));
+    check_status(c, c.stream);
+  });
+}
+
+int bg_pk_upload(bg_ctx* ctx, const bg_inputs* in, bg_pk** out) {
+  if (!ctx || !in || !out) return BG_E_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    PkDev* pk = pk_upload(ctx->c, *in);
+    *out = new bg_pk{pk, ctx};
+  });
+}
+
+void bg_pk_release(bg_pk* pk) {
+  if (!pk) return;
+  cudaSetDevice(pk->owner->c.device);
+  cudaStreamSynchronize(pk->owner->c.stream);
+  pk_free(pk->pk);
+  delete pk;
+}
+
+int bg_prove_resident(bg_ctx* ctx, bg_pk* pk, const uint32_t* witness16, const uint32_t* rs16, bg_proof* out,
+                      bg_phase_ms* times) {
+  if (!ctx || !pk || !witness16 || !rs16 || !out) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    prove_resident(ctx->c, *pk->pk, witness16, rs16, out, times, 0.0);
+  });
+}
+
+int bg_prove_host(bg_ctx* ctx, const bg_inputs* in, bg_proof* out, bg_phase_ms* times) {
+  if (!ctx || !in || !out) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    const auto t0 = std::chrono::steady_clock::now();
+    const Header h = parse_header(*in);
+    validate_inputs(*in, h, true);
+    PkDev* pk = pk_upload(ctx->c, *in);
+    const double up_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    try {
+      prove_resident(ctx->c, *pk, static_cast<const uint32_t*>(in->witness), static_cast<const uint32_t*>(in->rs),
+                     out, times, up_ms);
+    } catch (...) {
+      pk_free(pk);
+      throw;
+    }
+    pk_free(pk);
+  });
+}
+
+int bg_prove_dir(bg_ctx* ctx, const char* dir, bg_proof* out, bg_phase_ms* times) {
+  if (!ctx || !dir || !out) return BG_E_ARG;
+  return guard(ctx, [&] {
+    const auto t0 = std::chrono::steady_clock::now();
+    static const char* names[13] = {"header", "witness", "r1cs_a", "r1cs_b", "r1cs_c", "pk_g1", "pk_g2",
+                                    "pk_a",   "pk_b1",   "pk_b2",  "pk_h",   "pk_l",   "rs"};
+    std::vector<char> buf[13];
+    for (int i = 0; i < 13; i++) {
+      const std::string path = std::string(dir) + "/" + names[i] + ".bin";
+      if (!read_file(path, buf[i])) throw Error(BG_E_IO, "cannot read " + path);
+    }
+    bg_inputs in;
+    const void** ptrs[13] = {&in.header, &in.witness, &in.r1cs_a, &in.r1cs_b, &in.r1cs_c, &in.pk_g1, &in.pk_g2,
+                             &in.pk_a,   &in.pk_b1,   &in.pk_b2,  &in.pk_h,   &in.pk_l,   &in.rs};
+    size_t* sizes[13] = {&in.header_bytes, &in.witness_bytes, &in.r1cs_a_bytes, &in.r1cs_b_bytes,
+                         &in.r1cs_c_bytes, &in.pk_g1_bytes,   &in.pk_g2_bytes,  &in.pk_a_bytes,
+                         &in.pk_b1_bytes,  &in.pk_b2_bytes,   &in.pk_h_bytes,   &in.pk_l_bytes,
+                         &in.rs_bytes};
+    for (int i = 0; i < 13; i++) {
+      *ptrs[i] = buf[i].data();
+      *sizes[i] = buf[i].size();
+    }
+    cudaSetDevice(ctx->c.device);
+    const Header h = parse_header(in);
+    validate_inputs(in, h, true);
+    PkDev* pk = pk_upload(ctx->c, in);
+    const double load_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    try {
+      prove_resident(ctx->c, *pk, static_cast<const uint32_t*>(in.witness), static_cast<const uint32_t*>(in.rs),
+                     out, times, load_ms);
+    } catch (...) {
+      pk_free(pk);
+      throw;
+    }
+    pk_free(pk);
+  });
+}
+
+int bg_synth_square_chain(bg_ctx* ctx, uint32_t log2n, uint64_t seed, const char* dir) {
+  if (!ctx || !dir) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    synth_square_chain(ctx->c, log2n, seed, dir);
+  });
+}
+
+int bg_proof_format(const bg_proof* proof, char* buf, size_t buf_bytes) {
+  if (!proof || !buf) return BG_E_ARG;
+  return format_proof(proof, buf, buf_bytes);
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+// Shared host-side plumbing for the CUDA translation units: error handling, the per-context
+// workspace cache and the context record behind the C ABI handle.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/bg.h"
+
+namespace bg {
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define BG_CUDA(call)                                                                       \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      throw ::bg::Error(e_ == cudaErrorMemoryAllocation ? BG_E_OOM : BG_E_DEVICE,           \
+                        std::string(#call) + ": " + cudaGetErrorString(e_) + " at " +        \
+                            __FILE__ + ":" + std::to_string(__LINE__));                      \
+    }                                                                                       \
+  } while (0)
+
+// kernels launched by this library in this process (every launch site is followed by this check)
+extern std::atomic<uint64_t> g_launches;
+#define BG_CHECK_LAUNCH()      \
+  do {                         \
+    ::bg::g_launches++;        \
+    BG_CUDA(cudaGetLastError()); \
+  } while (0)
+
+// Device buffers cached per context by name: a call asks for `bytes` and gets a buffer of at
+// least that size, reused across calls (grown, never shrunk, until the context is freed).
+class Workspace {
+ public:
+  void* get(const std::string& name, size_t bytes) {
+    auto it = bufs_.find(name);
+    if (it != bufs_.end() && it->second.bytes >= bytes) return it->second.ptr;
+    if (it != bufs_.end()) {
+      cudaFree(it->second.ptr);
+      bufs_.erase(it);
+    }
+    void* p = nullptr;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw Error(BG_E_OOM, "device allocation of " + std::to_string(want) + " bytes for " + name + " failed: " +
+                                cudaGetErrorString(e));
+    }
+    bufs_[name] = {p, want};
+    return p;
+  }
+  template <class T>
+  T* get_t(const std::string& name, size_t count) {
+    return static_cast<T*>(get(name, count * sizeof(T)));
+  }
+  size_t bytes() const {
+    size_t s = 0;
+    for (auto& kv : bufs_) s += kv.second.bytes;
+    return s;
+  }
+  void clear() {
+    for (auto& kv : bufs_) cudaFree(kv.second.ptr);
+    bufs_.clear();
+  }
+  ~Workspace() { clear(); }
+
+ private:
+  struct Buf {
+    void* ptr;
+    size_t bytes;
+  };
+  std::map<std::string, Buf> bufs_;
+};
+
+// Pinned host staging buffer, grown on demand
+class PinnedBuf {
+ public:
+  void* get(size_t bytes) {
+    if (bytes > cap_) {
+      if (ptr_) cudaFreeHost(ptr_);
+      ptr_ = nullptr;
+      BG_CUDA(cudaMallocHost(&ptr_, bytes));
+      cap_ = bytes;
+    }
+    return ptr_;
+  }
+  ~PinnedBuf() {
+    if (ptr_) cudaFreeHost(ptr_);
+  }
+
+ private:
+  void* ptr_ = nullptr;
+  size_t cap_ = 0;
+};
+
+constexpr int kStreams = 6;
+
+// NTT tables for one domain size 2^L (device pointers into the context workspace)
+struct NttTables {
+  bool ready = false;
+  uint32_t* tw_fwd = nullptr;      // w^i, i < 2^(L-1), w of order 2^L (Montgomery)
+  uint32_t* tw_inv = nullptr;      // w^-i
+  int coset_bits = 0;              // a: coset powers split as lo[i & (2^a-1)] * hi[i >> a]
+  uint32_t* g_lo = nullptr;        // g^i, i < 2^a
+  uint32_t* gi_lo = nullptr;       // g^-i
+  uint32_t* g_hi = nullptr;        // g^(i 2^a)
+  uint32_t* g_hi_ninv = nullptr;   // n^-1 g^(i 2^a)
+  uint32_t* gi_hi_ninv = nullptr;  // n^-1 g^(-i 2^a)
+  uint32_t* ninv = nullptr;        // n^-1
+  uint32_t* zinv = nullptr;        // (g^n - 1)^-1
+};
+
+struct Ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;          // main stream: every public call is ordered on it
+  cudaStream_t side[kStreams] = {};       // concurrent MSMs inside a proof
+  cudaEvent_t ev_fork = nullptr;
+  cudaEvent_t ev_join[kStreams] = {};
+  Workspace ws;
+  PinnedBuf pinned[4];
+  std::string last_error;
+  uint32_t* d_status = nullptr;           // device-side error flags (see BG_DSTATUS_*)
+  std::map<int, NttTables> ntt_tabs;      // per domain size, built on first use
+  // scalar profiling of the last call: named phase durations in ms
+  std::vector<std::pair<std::string, float>> phases;
+};
+
+// device status flag bits
+enum : uint32_t {
+  BG_DSTATUS_SCALAR_RANGE = 1u,  // an MSM scalar had bit 254 or 255 set
+  BG_DSTATUS_CAPACITY = 2u,      // a bucket list overflowed its capacity
+  BG_DSTATUS_FORMAT = 4u,        // a wire word had bits above its 16-bit limb
+  BG_DSTATUS_COLUMN = 8u,        // an R1CS column index was outside the assignment
+};
+
+inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace bg

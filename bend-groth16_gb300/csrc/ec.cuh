@@ -1,0 +1,214 @@
+// Short Weierstrass curves y^2 = x^3 + b (a = 0) over Fq (G1) and Fq2 (G2) on the device.
+//
+// Affine points use the wire convention of the reference: infinity is (0, 0), which is not
+// on the curve (bend2/FORMAT.md:14-16, bend2/src/g1.bend:19-25).  Accumulators use
+// extended Jacobian "XYZZ" coordinates (x = X/ZZ, y = Y/ZZZ, ZZ^3 = ZZZ^2), infinity is
+// ZZ = 0.  Formulas are the Explicit-Formulas Database ones for XYZZ with a = 0:
+//   madd-2008-s (XYZZ + affine, 8M + 2S), add-2008-s (XYZZ + XYZZ, 12M + 2S),
+//   dbl-2008-s-1 (XYZZ, 6M + 3S), mdbl-2008-s (affine -> XYZZ double, 3M + 2S).
+// The reference's Jacobian madd-2007-bl / add-2007-bl / dbl-2009-l (bend2/src/g1.bend:76-172)
+// compute the same group law; only the projective representation differs, and every
+// result leaving the device is normalised (affine, or Jacobian with Z = 1).
+// Special cases (infinity, P == Q, P == -Q) are resolved by branches before the generic
+// formula; they are rare on random inputs, so the branch is almost never divergent.
+#pragma once
+#include "fp.cuh"
+
+namespace bg {
+
+template <class F>
+struct Affine {
+  F x, y;
+};
+
+template <class F>
+struct XYZZ {
+  F x, y, zz, zzz;
+};
+
+template <class F>
+BG_DEV bool is_inf(const Affine<F>& p) { return is_zero(p.x) && is_zero(p.y); }
+
+template <class F>
+BG_DEV bool is_inf(const XYZZ<F>& p) { return is_zero(p.zz); }
+
+template <class F>
+BG_DEV XYZZ<F> xyzz_inf() {
+  XYZZ<F> r;
+  r.x = field_one<F>();
+  r.y = field_one<F>();
+  r.zz = field_zero<F>();
+  r.zzz = field_zero<F>();
+  return r;
+}
+
+template <class F>
+BG_DEV XYZZ<F> xyzz_from_affine(const Affine<F>& p) {
+  if (is_inf(p)) return xyzz_inf<F>();
+  XYZZ<F> r;
+  r.x = p.x;
+  r.y = p.y;
+  r.zz = field_one<F>();
+  r.zzz = field_one<F>();
+  return r;
+}
+
+template <class F>
+BG_DEV Affine<F> affine_neg(const Affine<F>& p) {
+  Affine<F> r;
+  r.x = p.x;
+  r.y = neg(p.y);  // neg(0) = 0 keeps the (0, 0) infinity encoding
+  return r;
+}
+
+template <class F>
+BG_DEV XYZZ<F> xyzz_neg(const XYZZ<F>& p) {
+  XYZZ<F> r = p;
+  r.y = neg(p.y);
+  return r;
+}
+
+// 2P for affine P != infinity, y != 0 (mdbl-2008-s)
+template <class F>
+BG_DEV XYZZ<F> xyzz_dbl_affine(const Affine<F>& p) {
+  const F u = dbl(p.y);
+  const F v = sqr(u);
+  const F w = mul(u, v);
+  const F s = mul(p.x, v);
+  const F x2 = sqr(p.x);
+  const F m = add(dbl(x2), x2);
+  XYZZ<F> r;
+  r.x = sub(sqr(m), dbl(s));
+  r.y = sub(mul(m, sub(s, r.x)), mul(w, p.y));
+  r.zz = v;
+  r.zzz = w;
+  return r;
+}
+
+// 2P (dbl-2008-s-1)
+template <class F>
+BG_DEV XYZZ<F> xyzz_dbl(const XYZZ<F>& p) {
+  if (is_inf(p)) return p;
+  const F u = dbl(p.y);
+  const F v = sqr(u);
+  const F w = mul(u, v);
+  const F s = mul(p.x, v);
+  const F x2 = sqr(p.x);
+  const F m = add(dbl(x2), x2);
+  XYZZ<F> r;
+  r.x = sub(sqr(m), dbl(s));
+  r.y = sub(mul(m, sub(s, r.x)), mul(w, p.y));
+  r.zz = mul(v, p.zz);
+  r.zzz = mul(w, p.zzz);
+  return r;
+}
+
+// P + Q for XYZZ P and affine Q (madd-2008-s)
+template <class F>
+BG_DEV XYZZ<F> xyzz_madd(const XYZZ<F>& p, const Affine<F>& q) {
+  if (is_inf(q)) return p;
+  if (is_inf(p)) return xyzz_from_affine(q);
+  const F u2 = mul(q.x, p.zz);
+  const F s2 = mul(q.y, p.zzz);
+  const F pp_ = sub(u2, p.x);
+  const F r_ = sub(s2, p.y);
+  if (is_zero(pp_)) {
+    if (is_zero(r_)) return xyzz_dbl_affine(q);
+    return xyzz_inf<F>();
+  }
+  const F pp = sqr(pp_);
+  const F ppp = mul(pp_, pp);
+  const F qq = mul(p.x, pp);
+  XYZZ<F> r;
+  r.x = sub(sub(sqr(r_), ppp), dbl(qq));
+  r.y = sub(mul(r_, sub(qq, r.x)), mul(p.y, ppp));
+  r.zz = mul(p.zz, pp);
+  r.zzz = mul(p.zzz, ppp);
+  return r;
+}
+
+// P + Q for XYZZ P, Q (add-2008-s)
+template <class F>
+BG_DEV XYZZ<F> xyzz_add(const XYZZ<F>& p, const XYZZ<F>& q) {
+  if (is_inf(q)) return p;
+  if (is_inf(p)) return q;
+  const F u1 = mul(p.x, q.zz);
+  const F u2 = mul(q.x, p.zz);
+  const F s1 = mul(p.y, q.zzz);
+  const F s2 = mul(q.y, p.zzz);
+  const F pp_ = sub(u2, u1);
+  const F r_ = sub(s2, s1);
+  if (is_zero(pp_)) {
+    if (is_zero(r_)) return xyzz_dbl(p);
+    return xyzz_inf<F>();
+  }
+  const F pp = sqr(pp_);
+  const F ppp = mul(pp_, pp);
+  const F qq = mul(u1, pp);
+  XYZZ<F> r;
+  r.x = sub(sub(sqr(r_), ppp), dbl(qq));
+  r.y = sub(mul(r_, sub(qq, r.x)), mul(s1, ppp));
+  r.zz = mul(mul(p.zz, q.zz), pp);
+  r.zzz = mul(mul(p.zzz, q.zzz), ppp);
+  return r;
+}
+
+// ---------------------------------------------------------------- packed memory layout
+// G1 affine: x[8] y[8] (64 B).  G2 affine: x.c0 x.c1 y.c0 y.c1 (128 B).
+// XYZZ: x, y, zz, zzz (4 field elements).
+BG_DEV void load_elem(Fq& r, const uint32_t* src) { r = load_fp<FqParams>(src); }
+BG_DEV void load_elem(Fq2& r, const uint32_t* src) {
+  r.c0 = load_fp<FqParams>(src);
+  r.c1 = load_fp<FqParams>(src + 8);
+}
+BG_DEV void store_elem(uint32_t* dst, const Fq& x) { store_fp(dst, x); }
+BG_DEV void store_elem(uint32_t* dst, const Fq2& x) {
+  store_fp(dst, x.c0);
+  store_fp(dst + 8, x.c1);
+}
+
+template <class F>
+struct FieldWords;
+template <>
+struct FieldWords<Fq> {
+  static constexpr int value = 8;
+};
+template <>
+struct FieldWords<Fq2> {
+  static constexpr int value = 16;
+};
+
+template <class F>
+BG_DEV Affine<F> load_affine(const uint32_t* src) {
+  constexpr int W = FieldWords<F>::value;
+  Affine<F> p;
+  load_elem(p.x, src);
+  load_elem(p.y, src + W);
+  return p;
+}
+template <class F>
+BG_DEV void store_affine(uint32_t* dst, const Affine<F>& p) {
+  constexpr int W = FieldWords<F>::value;
+  store_elem(dst, p.x);
+  store_elem(dst + W, p.y);
+}
+template <class F>
+BG_DEV XYZZ<F> load_xyzz(const uint32_t* src) {
+  constexpr int W = FieldWords<F>::value;
+  XYZZ<F> p;
+  load_elem(p.x, src);
+  load_elem(p.y, src + W);
+  load_elem(p.zz, src + 2 * W);
+  load_elem(p.zzz, src + 3 * W);
+  return p;
+}
+template <class F>
+BG_DEV void store_xyzz(uint32_t* dst, const XYZZ<F>& p) {
+  constexpr int W = FieldWords<F>::value;
+  store_elem(dst, p.x);
+  store_elem(dst + W, p.y);
+  store_elem(dst + 2 * W, p.zz);
+  store_elem(dst + 3 * W, p.zzz);
+}
+
+}  // namespace bg

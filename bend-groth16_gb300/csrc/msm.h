@@ -1,0 +1,34 @@
+// MSM engine interface (see msm.cu)
+#pragma once
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace bg {
+
+struct MsmPlan {
+  int c = 0;                              // window bits (0: pick from n)
+  int W = 0;                              // windows
+  const uint32_t* d_window_sums = nullptr;  // W XYZZ points on the device
+  std::vector<uint32_t> host_window_sums;   // W XYZZ points after msm_fetch
+};
+
+int msm_pick_c(size_t n);
+void exclusive_scan(Workspace& ws, const std::string& tag, const uint32_t* d_in, uint32_t* d_out, size_t n,
+                    cudaStream_t st, int depth);
+
+// Enqueue every device phase of one MSM on `st`; scratch buffers are named by `tag` so that
+// concurrent MSMs on different streams use different memory.
+template <class F>
+void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
+                const uint32_t* d_scalars, size_t n, MsmPlan& plan);
+// Enqueue the copy of the window sums to the host.
+template <class F>
+void msm_fetch(cudaStream_t st, MsmPlan& plan);
+// After the stream is synchronised: Horner over windows, affine result (packed words,
+// 16 for G1, 32 for G2; all zero = infinity).
+template <class F>
+void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32);
+
+}  // namespace bg

@@ -1,0 +1,469 @@
+// The Groth16 prove pipeline on one device.
+//
+// Mirrors Pr.run (bend2/prove.bend:129-162): load (bend2/src/groth16.bend:238-254), evals
+// (Ev.matrix / matrix_a, groth16.bend:162-188, then Sc.canon, :214), qap (Pr.qap,
+// prove.bend:52-56), the five MSMs (prove.bend:64-117) and Groth.combine (groth16.bend:298-308).
+//
+// Device schedule (one context, one main stream + side streams):
+//   main:  witness H2D + repack -> evals (3 CSR SpMV) -> z canonical --fork--> qap_h -> h canonical -> msm_h
+//   side0: msm_a (pk_a, z)      side1: msm_b1 (pk_b1, z)     side2: msm_b2 (pk_b2, z, G2)
+//   side3: msm_l (pk_l, z[2..])
+// msm_a/b1/b2/l need only z and start while the QAP runs.  Each MSM ends with its window sums
+// on the host; the host runs the window Horner and the combine (a handful of scalar
+// multiplications; r*delta etc. are computed while the device works).
+#include <chrono>
+#include <cstring>
+#include <thread>
+
+#include "common.cuh"
+#include "ec.cuh"
+#include "host_ff.hpp"
+#include "msm.h"
+#include "ntt.h"
+#include "prims.h"
+#include "prove.h"
+
+namespace bg {
+
+using bgh::Aff;
+using bgh::Fe;
+using bgh::Fq2Ops;
+using bgh::FqOps;
+using bgh::Xyzz;
+
+// ---------------------------------------------------------------- evaluation vectors
+// Row i < N: sum_e coeff_e * z[col_e] over the CSR row (a coefficient equal to Montgomery one
+// skips the product, as Ev.ent.s2 does, groth16.bend:108-113).  Rows N .. N+ni-1 of A carry the
+// libsnark input-consistency entries a[N+i] = z[i] (groth16.bend:182-188); all other rows are 0.
+__global__ void k_evals(const uint32_t* __restrict__ offs, const uint32_t* __restrict__ cols,
+                        const uint32_t* __restrict__ coeffs, const uint32_t* __restrict__ z, uint32_t nz,
+                        uint32_t nrows, uint32_t ni_rows, size_t d, uint32_t* __restrict__ out,
+                        uint32_t* __restrict__ status) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d) return;
+  Fr acc = fp_zero<FrParams>();
+  if (i < nrows) {
+    const Fr one = fp_one<FrParams>();
+    for (uint32_t e = offs[i]; e < offs[i + 1]; e++) {
+      const uint32_t col = cols[e];
+      if (col >= nz) {
+        atomicOr(status, BG_DSTATUS_COLUMN);
+        continue;
+      }
+      const Fr zv = load_fp<FrParams>(z + 8 * (size_t)col);
+      const Fr cf = load_fp<FrParams>(coeffs + 8 * (size_t)e);
+      acc = add(acc, eq(cf, one) ? zv : mul(cf, zv));
+    }
+  } else if (i - nrows < ni_rows) {
+    acc = load_fp<FrParams>(z + 8 * (i - nrows));
+  }
+  store_fp(out + 8 * i, acc);
+}
+
+// split raw CSR entries (u32 col, 16 wire words) into cols[] and packed coefficients
+__global__ void k_csr_split(const uint32_t* __restrict__ raw, size_t nnz, uint32_t* __restrict__ cols,
+                            uint32_t* __restrict__ coeffs, uint32_t* __restrict__ status) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nnz) return;
+  const uint32_t* src = raw + 17 * e;
+  cols[e] = src[0];
+  uint32_t hi = 0;
+  uint32_t w[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const uint32_t lo = src[1 + 2 * j], up = src[2 + 2 * j];
+    hi |= (lo | up) >> 16;
+    w[j] = (lo & 0xffffu) | (up << 16);
+  }
+  if (hi) atomicOr(status, BG_DSTATUS_FORMAT);
+#pragma unroll
+  for (int j = 0; j < 8; j++) coeffs[8 * e + j] = w[j];
+}
+
+// ---------------------------------------------------------------- input validation (host)
+static const uint32_t* words(const void* p) { return static_cast<const uint32_t*>(p); }
+
+Header parse_header(const bg_inputs& in) {
+  if (!in.header || in.header_bytes != 32) throw Error(BG_E_FORMAT, "header.bin must hold 8 u32 words");
+  const uint32_t* w = words(in.header);
+  Header h{w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7]};
+  const uint64_t d = 1ull << h.lg;
+  if (h.lg > 27) throw Error(BG_E_FORMAT, "header: domain_log2 above the 2-adic limit");
+  if ((uint64_t)h.nc + h.ni > d) throw Error(BG_E_FORMAT, "header: constraints + instance exceed the domain");
+  if (h.na != h.ni + h.nw || h.nb != h.ni + h.nw) throw Error(BG_E_FORMAT, "header: n_a/n_b must equal num_instance + num_witness");
+  if (h.nh > d) throw Error(BG_E_FORMAT, "header: n_h exceeds the domain");
+  if (h.nl > h.nw) throw Error(BG_E_FORMAT, "header: n_l exceeds num_witness");
+  if (h.ni < 1) throw Error(BG_E_FORMAT, "header: num_instance must be >= 1");
+  return h;
+}
+
+static void need(size_t got, size_t want, const char* what) {
+  if (got != want)
+    throw Error(BG_E_FORMAT, std::string(what) + ": " + std::to_string(got) + " bytes, header implies " +
+                                 std::to_string(want));
+}
+
+static void check_csr(const void* p, size_t bytes, uint32_t nc, const char* what, uint32_t& nnz) {
+  if (!p || bytes < 4) throw Error(BG_E_FORMAT, std::string(what) + ": missing");
+  const uint32_t* w = words(p);
+  nnz = w[0];
+  need(bytes, 4ull * (1 + (size_t)nc + 1 + 17ull * nnz), what);
+  const uint32_t* offs = w + 1;
+  if (offs[0] != 0 || offs[nc] != nnz) throw Error(BG_E_FORMAT, std::string(what) + ": offsets do not span nnz");
+  for (uint32_t i = 0; i < nc; i++)
+    if (offs[i + 1] < offs[i]) throw Error(BG_E_FORMAT, std::string(what) + ": offsets decrease");
+}
+
+void validate_inputs(const bg_inputs& in, const Header& h, bool need_witness) {
+  need(in.pk_g1_bytes, 3 * 128, "pk_g1.bin");
+  need(in.pk_g2_bytes, 2 * 256, "pk_g2.bin");
+  need(in.pk_a_bytes, (size_t)h.na * 128, "pk_a.bin");
+  need(in.pk_b1_bytes, (size_t)h.nb * 128, "pk_b1.bin");
+  need(in.pk_b2_bytes, (size_t)h.nb * 256, "pk_b2.bin");
+  need(in.pk_h_bytes, (size_t)h.nh * 128, "pk_h.bin");
+  need(in.pk_l_bytes, (size_t)h.nl * 128, "pk_l.bin");
+  if (need_witness) {
+    need(in.witness_bytes, (size_t)(h.ni + h.nw) * 64, "witness.bin");
+    need(in.rs_bytes, 2 * 64, "rs.bin");
+  }
+  uint32_t nnz;
+  check_csr(in.r1cs_a, in.r1cs_a_bytes, h.nc, "r1cs_a.bin", nnz);
+  check_csr(in.r1cs_b, in.r1cs_b_bytes, h.nc, "r1cs_b.bin", nnz);
+  check_csr(in.r1cs_c, in.r1cs_c_bytes, h.nc, "r1cs_c.bin", nnz);
+}
+
+// ---------------------------------------------------------------- proving key upload
+template <class H>
+static Aff<H> host_affine_from_wire(const uint32_t* w16) {
+  Aff<H> a;
+  uint32_t packed[2 * H::WORDS];
+  for (int i = 0; i < 2 * H::WORDS; i++) {
+    packed[i] = (w16[2 * i] & 0xffffu) | (w16[2 * i + 1] << 16);
+  }
+  return bgh::aff_from_words32<H>(packed);
+}
+
+static void* dmalloc(size_t bytes) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes < 256 ? 256 : bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(BG_E_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+  }
+  return p;
+}
+
+// copy `bytes` of host memory to a device buffer through the context's pinned staging
+static void h2d(Ctx& ctx, int slot, void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, src) == cudaSuccess && attr.type == cudaMemoryTypeHost) {
+    BG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    return;
+  }
+  cudaGetLastError();
+  // pageable source: stage in chunks through pinned memory
+  const size_t chunk = 64ull << 20;
+  char* pin = static_cast<char*>(ctx.pinned[slot].get(std::min(bytes, chunk) * 2));
+  const char* s = static_cast<const char*>(src);
+  char* d = static_cast<char*>(dst);
+  size_t off = 0;
+  int half = 0;
+  cudaEvent_t done[2];
+  BG_CUDA(cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming));
+  BG_CUDA(cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming));
+  bool used[2] = {false, false};
+  while (off < bytes) {
+    const size_t len = std::min(chunk, bytes - off);
+    char* buf = pin + (size_t)half * std::min(bytes, chunk);
+    if (used[half]) BG_CUDA(cudaEventSynchronize(done[half]));
+    memcpy(buf, s + off, len);
+    BG_CUDA(cudaMemcpyAsync(d + off, buf, len, cudaMemcpyHostToDevice, st));
+    BG_CUDA(cudaEventRecord(done[half], st));
+    used[half] = true;
+    off += len;
+    half ^= 1;
+  }
+  BG_CUDA(cudaEventSynchronize(done[0]));
+  BG_CUDA(cudaEventSynchronize(done[1]));
+  cudaEventDestroy(done[0]);
+  cudaEventDestroy(done[1]);
+}
+
+static void upload_points(Ctx& ctx, const void* src, size_t n, int words_per_point, uint32_t*& d_out,
+                          cudaStream_t st) {
+  // wire words -> staging on device -> packed
+  const size_t wire_words = n * words_per_point;
+  d_out = static_cast<uint32_t*>(dmalloc(wire_words / 2 * 4));
+  uint32_t* stage = ctx.ws.get_t<uint32_t>("upload.stage", wire_words);
+  h2d(ctx, 0, stage, src, wire_words * 4, st);
+  wire_to_packed(st, stage, d_out, wire_words / 16, ctx.d_status);
+}
+
+static void upload_csr(Ctx& ctx, const void* src, uint32_t nc, CsrDev& out, cudaStream_t st) {
+  const uint32_t* w = words(src);
+  out.nnz = w[0];
+  out.offs = static_cast<uint32_t*>(dmalloc(((size_t)nc + 1) * 4));
+  out.cols = static_cast<uint32_t*>(dmalloc((size_t)out.nnz * 4));
+  out.coeffs = static_cast<uint32_t*>(dmalloc((size_t)out.nnz * 32));
+  h2d(ctx, 0, out.offs, w + 1, ((size_t)nc + 1) * 4, st);
+  if (out.nnz) {
+    uint32_t* stage = ctx.ws.get_t<uint32_t>("upload.csr", 17ull * out.nnz);
+    h2d(ctx, 0, stage, w + 2 + nc, 17ull * out.nnz * 4, st);
+    k_csr_split<<<ceil_div(out.nnz, 256), 256, 0, st>>>(stage, out.nnz, out.cols, out.coeffs, ctx.d_status);
+    BG_CHECK_LAUNCH();
+  }
+}
+
+void check_status(Ctx& ctx, cudaStream_t st) {
+  uint32_t s = 0;
+  BG_CUDA(cudaMemcpyAsync(&s, ctx.d_status, 4, cudaMemcpyDeviceToHost, st));
+  BG_CUDA(cudaStreamSynchronize(st));
+  if (s) {
+    BG_CUDA(cudaMemsetAsync(ctx.d_status, 0, 4, st));
+    BG_CUDA(cudaStreamSynchronize(st));
+    if (s & BG_DSTATUS_SCALAR_RANGE) throw Error(BG_E_ARG, "an MSM scalar is not below 2^254 (not a canonical Fr)");
+    if (s & BG_DSTATUS_FORMAT) throw Error(BG_E_FORMAT, "a wire word has bits above its 16-bit limb");
+    if (s & BG_DSTATUS_COLUMN) throw Error(BG_E_FORMAT, "an R1CS column index is outside the assignment");
+    throw Error(BG_E_DEVICE, "device status flag " + std::to_string(s));
+  }
+}
+
+PkDev* pk_upload(Ctx& ctx, const bg_inputs& in) {
+  const Header h = parse_header(in);
+  validate_inputs(in, h, false);
+  PkDev* pk = new PkDev();
+  pk->h = h;
+  try {
+    cudaStream_t st = ctx.stream;
+    upload_points(ctx, in.pk_a, h.na, 32, pk->pa, st);
+    upload_points(ctx, in.pk_b1, h.nb, 32, pk->pb1, st);
+    upload_points(ctx, in.pk_b2, h.nb, 64, pk->pb2, st);
+    upload_points(ctx, in.pk_h, h.nh, 32, pk->ph, st);
+    upload_points(ctx, in.pk_l, h.nl, 32, pk->pl, st);
+    upload_csr(ctx, in.r1cs_a, h.nc, pk->ca, st);
+    upload_csr(ctx, in.r1cs_b, h.nc, pk->cb, st);
+    upload_csr(ctx, in.r1cs_c, h.nc, pk->cc, st);
+    const uint32_t* g1 = words(in.pk_g1);
+    const uint32_t* g2 = words(in.pk_g2);
+    pk->alpha = host_affine_from_wire<FqOps>(g1);
+    pk->beta = host_affine_from_wire<FqOps>(g1 + 32);
+    pk->delta = host_affine_from_wire<FqOps>(g1 + 64);
+    pk->beta2 = host_affine_from_wire<Fq2Ops>(g2);
+    pk->delta2 = host_affine_from_wire<Fq2Ops>(g2 + 64);
+    check_status(ctx, st);
+  } catch (...) {
+    pk_free(pk);
+    throw;
+  }
+  return pk;
+}
+
+void pk_free(PkDev* pk) {
+  if (!pk) return;
+  for (uint32_t* p : {pk->pa, pk->pb1, pk->pb2, pk->ph, pk->pl, pk->ca.offs, pk->ca.cols, pk->ca.coeffs,
+                      pk->cb.offs, pk->cb.cols, pk->cb.coeffs, pk->cc.offs, pk->cc.cols, pk->cc.coeffs})
+    if (p) cudaFree(p);
+  delete pk;
+}
+
+// ---------------------------------------------------------------- combine (host)
+static void scalar_from_mont_wire(const uint32_t* w16, uint64_t out[4]) {
+  const Fe m = bgh::fe_from_words16(w16);
+  const Fe c = bgh::fe_from_mont(bgh::FR, m);
+  for (int i = 0; i < 4; i++) out[i] = c.v[i];
+}
+
+template <class H>
+static void wire_from_affine(uint32_t* w16, const Aff<H>& a) {
+  uint32_t packed[2 * H::WORDS];
+  bgh::aff_to_words32<H>(packed, a);
+  for (int i = 0; i < 2 * H::WORDS; i++) {
+    w16[2 * i] = packed[i] & 0xffffu;
+    w16[2 * i + 1] = packed[i] >> 16;
+  }
+}
+
+struct Timer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  void start(cudaStream_t st) {
+    BG_CUDA(cudaEventCreate(&a));
+    BG_CUDA(cudaEventCreate(&b));
+    BG_CUDA(cudaEventRecord(a, st));
+  }
+  void stop(cudaStream_t st) { BG_CUDA(cudaEventRecord(b, st)); }
+  double ms() {
+    float t = 0;
+    if (a && b) cudaEventElapsedTime(&t, a, b);
+    return t;
+  }
+  ~Timer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32_t* rs16, bg_proof* out,
+                    bg_phase_ms* times, double load_ms_before) {
+  const auto t_wall0 = std::chrono::steady_clock::now();
+  const Header& h = pk.h;
+  const size_t d = size_t(1) << h.lg;
+  const size_t nz = (size_t)h.ni + h.nw;
+  cudaStream_t st = ctx.stream;
+  Workspace& ws = ctx.ws;
+
+  // ---- load: witness to the device
+  Timer t_load, t_evals, t_qap, t_msm[5];
+  t_load.start(st);
+  uint32_t* z_wire = ws.get_t<uint32_t>("prove.z_wire", nz * 16);
+  uint32_t* z = ws.get_t<uint32_t>("prove.z", nz * 8);
+  uint32_t* zc = ws.get_t<uint32_t>("prove.zc", nz * 8);
+  h2d(ctx, 1, z_wire, witness16, nz * 64, st);
+  wire_to_packed(st, z_wire, z, nz, ctx.d_status);
+  t_load.stop(st);
+
+  // ---- evals + canonical scalars
+  t_evals.start(st);
+  uint32_t* ea = ws.get_t<uint32_t>("prove.ea", d * 8);
+  uint32_t* eb = ws.get_t<uint32_t>("prove.eb", d * 8);
+  uint32_t* ec = ws.get_t<uint32_t>("prove.ec", d * 8);
+  const CsrDev* m[3] = {&pk.ca, &pk.cb, &pk.cc};
+  uint32_t* ev[3] = {ea, eb, ec};
+  for (int k = 0; k < 3; k++) {
+    k_evals<<<ceil_div(d, 128), 128, 0, st>>>(m[k]->offs, m[k]->cols, m[k]->coeffs, z, (uint32_t)nz, h.nc,
+                                              k == 0 ? h.ni : 0, d, ev[k], ctx.d_status);
+    BG_CHECK_LAUNCH();
+  }
+  fr_from_mont(st, z, zc, nz);
+  t_evals.stop(st);
+
+  // ---- fork the four MSMs that only need z
+  BG_CUDA(cudaEventRecord(ctx.ev_fork, st));
+  MsmPlan plan[5];
+  struct Job {
+    int stream;
+    const char* tag;
+    bool g2;
+    const uint32_t* pts;
+    const uint32_t* sc;
+    size_t n;
+  };
+  const Job jobs[4] = {{0, "msm_a", false, pk.pa, zc, h.na},
+                       {1, "msm_b1", false, pk.pb1, zc, h.nb},
+                       {2, "msm_b2", true, pk.pb2, zc, h.nb},
+                       {3, "msm_l", false, pk.pl, zc + 8 * (size_t)h.ni, h.nl}};
+  const int plan_idx[4] = {0, 1, 2, 4};  // a, b1, b2, l; index 3 is msm_h
+  for (int j = 0; j < 4; j++) {
+    cudaStream_t s = ctx.side[jobs[j].stream];
+    BG_CUDA(cudaStreamWaitEvent(s, ctx.ev_fork, 0));
+    MsmPlan& p = plan[plan_idx[j]];
+    t_msm[plan_idx[j]].start(s);
+    if (jobs[j].g2) {
+      msm_launch<Fq2>(ctx, s, jobs[j].tag, jobs[j].pts, jobs[j].sc, jobs[j].n, p);
+      msm_fetch<Fq2>(s, p);
+    } else {
+      msm_launch<Fq>(ctx, s, jobs[j].tag, jobs[j].pts, jobs[j].sc, jobs[j].n, p);
+      msm_fetch<Fq>(s, p);
+    }
+    t_msm[plan_idx[j]].stop(s);
+  }
+
+  // ---- QAP on the main stream, then msm_h
+  t_qap.start(st);
+  uint32_t* hh = ws.get_t<uint32_t>("prove.h", d * 8);
+  uint32_t* hc = ws.get_t<uint32_t>("prove.hc", d * 8);
+  qap_h_run(ctx, st, ea, eb, ec, hh, h.lg);
+  fr_from_mont(st, hh, hc, h.nh);
+  t_qap.stop(st);
+  t_msm[3].start(st);
+  msm_launch<Fq>(ctx, st, "msm_h", pk.ph, hc, h.nh, plan[3]);
+  msm_fetch<Fq>(st, plan[3]);
+  t_msm[3].stop(st);
+
+  // ---- host work that needs no MSM result, overlapped with the device
+  uint64_t r[4], s[4], rs[4];
+  scalar_from_mont_wire(rs16, r);
+  scalar_from_mont_wire(rs16 + 16, s);
+  {
+    const Fe rm = bgh::fe_from_words16(rs16), sm = bgh::fe_from_words16(rs16 + 16);
+    const Fe prod = bgh::fe_from_mont(bgh::FR, bgh::fe_mul(bgh::FR, rm, sm));
+    for (int i = 0; i < 4; i++) rs[i] = prod.v[i];
+  }
+  const Xyzz<FqOps> dj = bgh::xyzz_from(pk.delta);
+  const Xyzz<Fq2Ops> dj2 = bgh::xyzz_from(pk.delta2);
+  const Xyzz<FqOps> r_delta = bgh::xyzz_mul(dj, r);
+  const Xyzz<FqOps> s_delta = bgh::xyzz_mul(dj, s);
+  const Xyzz<FqOps> rs_delta = bgh::xyzz_mul(dj, rs);
+  const Xyzz<Fq2Ops> s_delta2 = bgh::xyzz_mul(dj2, s);
+
+  // ---- join
+  for (int j = 0; j < 4; j++) BG_CUDA(cudaStreamSynchronize(ctx.side[jobs[j].stream]));
+  BG_CUDA(cudaStreamSynchronize(st));
+  check_status(ctx, st);
+  uint32_t res[5][32];
+  msm_finish<Fq>(plan[0], res[0]);
+  msm_finish<Fq>(plan[1], res[1]);
+  msm_finish<Fq2>(plan[2], res[2]);
+  msm_finish<Fq>(plan[3], res[3]);
+  msm_finish<Fq>(plan[4], res[4]);
+
+  // ---- combine (groth16.bend:298-308):
+  // A = alpha + mA + r delta; B1 = beta + mB1 + s delta; B2 = beta2 + mB2 + s delta2;
+  // C = s A + r B1 - r s delta + (mL + mH)
+  auto g1 = [](const uint32_t* w) { return bgh::xyzz_from(bgh::aff_from_words32<FqOps>(w)); };
+  const Xyzz<FqOps> A = bgh::xyzz_add(bgh::xyzz_add(g1(res[0]), r_delta), bgh::xyzz_from(pk.alpha));
+  const Xyzz<FqOps> B1 = bgh::xyzz_add(bgh::xyzz_add(g1(res[1]), s_delta), bgh::xyzz_from(pk.beta));
+  const Xyzz<Fq2Ops> B2 = bgh::xyzz_add(
+      bgh::xyzz_add(bgh::xyzz_from(bgh::aff_from_words32<Fq2Ops>(res[2])), s_delta2), bgh::xyzz_from(pk.beta2));
+  const Xyzz<FqOps> C = bgh::xyzz_add(
+      bgh::xyzz_add(bgh::xyzz_mul(A, s), bgh::xyzz_mul(B1, r)),
+      bgh::xyzz_add(bgh::xyzz_neg(rs_delta), bgh::xyzz_add(g1(res[4]), g1(res[3]))));
+  wire_from_affine<FqOps>(out->a, bgh::xyzz_to_affine(A));
+  wire_from_affine<Fq2Ops>(out->b, bgh::xyzz_to_affine(B2));
+  wire_from_affine<FqOps>(out->c, bgh::xyzz_to_affine(C));
+
+  if (times) {
+    times->load = load_ms_before + t_load.ms();
+    times->evals = t_evals.ms();
+    times->qap = t_qap.ms();
+    times->msm_a = t_msm[0].ms();
+    times->msm_b1 = t_msm[1].ms();
+    times->msm_b2 = t_msm[2].ms();
+    times->msm_h = t_msm[3].ms();
+    times->msm_l = t_msm[4].ms();
+    times->total =
+        load_ms_before +
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
+  }
+}
+
+// ---------------------------------------------------------------- proof text
+int format_proof(const bg_proof* p, char* buf, size_t cap) {
+  auto hex = [](const uint32_t* w16, bool mont_fq, char* o) {
+    Fe v = bgh::fe_from_words16(w16);
+    if (mont_fq) v = bgh::fe_from_mont(bgh::FQ, v);
+    o += sprintf(o, "0x");
+    for (int i = 3; i >= 0; i--) o += sprintf(o, "%016llx", (unsigned long long)v.v[i]);
+    return o;
+  };
+  if (cap < 600) return BG_E_ARG;
+  char* o = buf;
+  o += sprintf(o, "A ");
+  o = hex(p->a, true, o);
+  *o++ = ' ';
+  o = hex(p->a + 16, true, o);
+  o += sprintf(o, "\nB ");
+  for (int i = 0; i < 4; i++) {
+    o = hex(p->b + 16 * i, true, o);
+    *o++ = i < 3 ? ' ' : '\n';
+  }
+  o += sprintf(o, "C ");
+  o = hex(p->c, true, o);
+  *o++ = ' ';
+  o = hex(p->c + 16, true, o);
+  *o++ = '\n';
+  *o = 0;
+  return BG_OK;
+}
+
+}  // namespace bg

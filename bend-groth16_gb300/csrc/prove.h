@@ -1,0 +1,38 @@
+// Prover pipeline interface (see prove.cu)
+#pragma once
+#include "common.cuh"
+#include "host_ff.hpp"
+
+namespace bg {
+
+// header.bin (bend2/FORMAT.md:16; bend2/src/groth16.bend:13-14)
+struct Header {
+  uint32_t nc, ni, nw, lg, na, nb, nh, nl;
+};
+
+struct CsrDev {
+  uint32_t nnz = 0;
+  uint32_t* offs = nullptr;    // nc + 1 row offsets
+  uint32_t* cols = nullptr;    // nnz column indexes
+  uint32_t* coeffs = nullptr;  // nnz packed Fr coefficients (Montgomery)
+};
+
+// device-resident proving key + circuit
+struct PkDev {
+  Header h{};
+  uint32_t *pa = nullptr, *pb1 = nullptr, *pb2 = nullptr, *ph = nullptr, *pl = nullptr;  // packed affine
+  CsrDev ca, cb, cc;
+  bgh::Aff<bgh::FqOps> alpha, beta, delta;
+  bgh::Aff<bgh::Fq2Ops> beta2, delta2;
+};
+
+Header parse_header(const bg_inputs& in);
+void validate_inputs(const bg_inputs& in, const Header& h, bool need_witness);
+PkDev* pk_upload(Ctx& ctx, const bg_inputs& in);
+void pk_free(PkDev* pk);
+void check_status(Ctx& ctx, cudaStream_t st);
+void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32_t* rs16, bg_proof* out,
+                    bg_phase_ms* times, double load_ms_before);
+int format_proof(const bg_proof* p, char* buf, size_t cap);
+
+}  // namespace bg

@@ -1,0 +1,77 @@
+"""Whole proofs: the golden SquareChain fixtures must reproduce proof_ref bit for bit (the
+role of bend2/tests/test_prove.sh), through every entry point (directory, host buffers,
+resident key, the prove_bin CLI); synthetic instances are checked in the exponent."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import bendg
+import oracle_io
+from conftest import GOLDEN, ROOT
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("k", [4, 10])
+def test_prove_dir_equals_proof_ref(ctx, k):
+    d = os.path.join(GOLDEN, "k%d" % k)
+    proof, t = ctx.prove_dir(d)
+    assert ctx.proof_text(proof) == open(os.path.join(d, "proof_ref.txt")).read()
+    assert all(v >= 0 for v in t.values())
+
+
+@pytest.mark.parametrize("k", [4, 10])
+def test_prove_host_and_resident_agree(ctx, k):
+    d = os.path.join(GOLDEN, "k%d" % k)
+    want = open(os.path.join(d, "proof_ref.txt")).read()
+    files = bendg.HostFiles(d, pinned=(k == 10))
+    proof, _ = ctx.prove_host(files)
+    assert ctx.proof_text(proof) == want
+    key = ctx.pk_upload(files)
+    for _ in range(2):  # repeated proofs against the resident key
+        proof, _ = key.prove(files.words("witness"), files.words("rs"))
+        assert ctx.proof_text(proof) == want
+    key.release()
+
+
+def test_prove_bin_cli(built_lib):
+    d = os.path.join(GOLDEN, "k4")
+    env = dict(os.environ, BENDG_DATA=d, BENDG_GPU="1")
+    out = subprocess.run([bendg.PROVE_BIN], env=env, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.splitlines()
+    assert "\n".join(lines[:3]) + "\n" == open(os.path.join(d, "proof_ref.txt")).read()
+    assert [ln.split()[1] for ln in lines[3:]] == list(bendg.PHASES)
+
+
+def test_prove_bin_missing_dir(built_lib):
+    env = dict(os.environ, BENDG_DATA="/nonexistent/dir")
+    out = subprocess.run([bendg.PROVE_BIN], env=env, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 1 and "cannot read" in out.stderr
+
+
+def test_truncated_file_rejected(ctx, tmp_path):
+    import shutil
+    d = os.path.join(GOLDEN, "k4")
+    for f in os.listdir(d):
+        shutil.copy(os.path.join(d, f), tmp_path / f)
+    data = open(tmp_path / "pk_h.bin", "rb").read()
+    open(tmp_path / "pk_h.bin", "wb").write(data[:-128])
+    with pytest.raises(bendg.BgError) as e:
+        ctx.prove_dir(str(tmp_path))
+    assert e.value.status == bendg.BG_E_FORMAT
+    proof, _ = ctx.prove_dir(d)  # context still usable
+    assert ctx.proof_text(proof) == open(os.path.join(d, "proof_ref.txt")).read()
+
+
+@pytest.mark.parametrize("log2n", [6, 12, 16])
+def test_synthetic_instance_trapdoor(ctx, tmp_path, log2n):
+    path = str(tmp_path / ("sq%d" % log2n))
+    ctx.synth_square_chain(log2n, 1234 + log2n, path)
+    data = oracle_io.load_dir(path)
+    trap = oracle_io.trapdoor_from_bin(data["trapdoor"])
+    proof, _ = ctx.prove_dir(path)
+    pts = oracle_io.parse_proof_text(ctx.proof_text(proof))
+    assert oracle_io.square_chain_trapdoor_check(data, trap, pts)
