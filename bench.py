@@ -1,0 +1,413 @@
+#!/usr/bin/env python3
+"""Benchmark of the Groth16/BN254 prover core on GB300: SquareChain(2^18) ms/proof.
+
+Workload (one step = one complete proof, all five MSMs and the QAP NTTs): the seeded
+synthetic SquareChain(2^18) instance (bend2/FORMAT.md files; N = 2^18 constraints,
+d = 2^19 domain, n_a = n_b = 2^18+2, n_h = 2^19-1, n_l = 2^18), generated once per box and
+cached.  No public dataset is involved; the instance has the shapes of the reference's K=18
+runs (bend2/bench/prover_results.md:59).
+
+  value  ms/proof with the proving key and the witness resident in HBM before timing
+         (bg_pk_upload + a device copy of witness.bin), CUDA events on the library's stream,
+         L2 flushed (512 MiB write) before every step outside the timed events.
+  e2e    ms/proof through bg_prove_host with every .bin file in pinned host memory: the whole
+         upload (all files), the proof and the result reads are inside the timed region.
+  roofline  the dominant kernel's algorithmic 32-bit multiply-adds per launch over its
+         CUDA-event duration, against the IMAD rate measured by the library's probe.
+  cpu_baseline  the C restatement in oracle/ (the reference's Bend/Rust CPU paths cannot
+         run here), all host threads, one proof of the same instance, rank 0 at N=1.
+
+`--impl reference` times that CPU restatement alone (rank 0; other ranks exit 0).
+Multi-GPU: replicas only (every rank proves its own copy; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "bend-groth16_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "SquareChain 2^18 ms/proof"
+UNIT = "ms/proof"
+# the reference's own GPU path (Bend 2 CUDA, RTX 5090) at K=18, T total
+REF_GPU_K18_MS = 56083.0
+FQ_MUL_IMAD = 264      # yardstick: 32-bit multiply-adds per 8x32-bit CIOS Fq product
+MADD_FQ_MULS = 11      # yardstick: Fq products per G1 mixed add (madd-2007-bl, 7M + 4S)
+MADD_G2_FQ_MULS = 29   # yardstick: Fq products per G2 mixed add (7*3 + 4*2 Karatsuba)
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--log2n", type=int, default=18)
+    ap.add_argument("--seed", type=int, default=18181818)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-primitives", action="store_true")
+    ap.add_argument("--data-root", default=os.environ.get("BG_BENCH_DATA", "/tmp/bg_bench"))
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- distributed plumbing
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def aggregate_ms_per_proof(times_ms_per_rank_max: float, world: int, steps: int) -> float:
+    """whole-job ms/proof: the slowest rank's time over all proofs of all ranks"""
+    return times_ms_per_rank_max / (world * steps)
+
+
+# ---------------------------------------------------------------- workload
+def instance_dir(args) -> str:
+    return os.path.join(args.data_root, "sq%d_s%d" % (args.log2n, args.seed))
+
+
+def ensure_instance(args, dist: Dist, generator) -> str:
+    path = instance_dir(args)
+    marker = os.path.join(path, "COMPLETE")
+    if dist.rank == 0 and not os.path.exists(marker):
+        os.makedirs(path, exist_ok=True)
+        generator(args.log2n, args.seed, path)
+        open(marker, "w").write("ok\n")
+    dist.barrier()
+    return path
+
+
+def window_counts(L, n):
+    c = L.bg_msm_window_bits(n)
+    return c, 254 // c + 1
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region"""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        rows = [[c.strip() for c in ln.split(",")] for ln in out.splitlines() if ln.strip()]
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = set()
+        for r in rows:
+            for i, nm in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args, dist: Dist):
+    import numpy as np
+    import torch
+
+    import bendg
+    torch.cuda.set_device(dist.local)
+    ctx = bendg.Context(dist.local)
+    L = bendg.lib()
+    path = ensure_instance(args, dist, lambda k, s, p: ctx.synth_square_chain(k, s, p))
+    files = bendg.HostFiles(path, pinned=True)
+    hdr = files.words("header")
+    nc, ni, nw, lg, na, nb, nh, nl = (int(v) for v in hdr[:8])
+
+    # resident proving key + device witness (inputs in HBM before the timed region)
+    key = ctx.pk_upload(files)
+    wit = torch.from_numpy(files.words("witness").astype(np.int64).astype(np.int32)).cuda()
+    rs = files.words("rs").copy()
+    rs_ptr = rs.ctypes.data
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    ext = torch.cuda.ExternalStream(ctx.stream)
+
+    def step_resident():
+        return key.prove_ptr(wit.data_ptr(), rs_ptr)
+
+    for _ in range(max(3, args.warmup)):
+        step_resident()
+    # IMAD peak of this GPU, measured before the timed region
+    ops, ms = ctx.probe_imad(0, 4096)
+    imad_peak = ops / (ms * 1e-3)
+    ops_f, ms_f = ctx.probe_imad(1, 256)
+    fqmul_rate = ops_f / (ms_f * 1e-3)
+
+    ctx.profile(True)
+    launches0 = ctx.launches()
+    clocks = ClockSampler(dist.local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    step_ms, phases = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        _, t = step_resident()
+        e1.record(ext)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        phases.append(t)
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    launches = ctx.launches() - launches0
+    total = dist.max(sum(step_ms))
+    value = aggregate_ms_per_proof(total, dist.world, args.steps)
+
+    # roofline of the dominant kernel (the one with the largest summed time)
+    fams = ["msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_reduce_g1", "msm_reduce_g2", "msm_digits",
+            "msm_scatter", "ntt_pass"]
+    stats = {f: ctx.kernel_stats(f) for f in fams}
+    ctx.profile(False)
+    dom = max(stats, key=lambda f: stats[f][1])
+    g1_sizes = [na, nb, nh, nl]
+    entries_g1 = sum(n * window_counts(L, n)[1] for n in g1_sizes)
+    entries_g2 = nb * window_counts(L, nb)[1]
+    work = {"msm_bucket_acc_g1": entries_g1 * MADD_FQ_MULS * FQ_MUL_IMAD,
+            "msm_bucket_acc_g2": entries_g2 * MADD_G2_FQ_MULS * FQ_MUL_IMAD}
+    roof = None
+    if dom in work:
+        nl_, tms = stats[dom]
+        per_launch_work = work[dom] * args.steps / max(1, nl_)
+        avg_ms = tms / max(1, nl_)
+        achieved = per_launch_work / (avg_ms * 1e-3) / 1e9
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+        if os.path.exists(tf):
+            traffic = json.load(open(tf)).get(dom, {}).get("bytes_per_launch")
+        roof = {"kernel": dom, "bound": "imad", "achieved": round(achieved, 1), "peak": round(imad_peak / 1e9, 1),
+                "unit": "Gimad/s", "frac": round(achieved / (imad_peak / 1e9), 4), "traffic": traffic,
+                "work_per_launch": per_launch_work, "avg_launch_ms": round(avg_ms, 4),
+                "peak_source": "bg_probe_imad on this GPU (32-bit mad.lo/mad.hi chains)",
+                "work_model": "entries x %d Fq-mul (G2: %d) x %d IMAD" % (MADD_FQ_MULS, MADD_G2_FQ_MULS, FQ_MUL_IMAD)}
+    kernel_ms = {f: {"launches": v[0], "ms_per_proof": round(v[1] / args.steps, 3)} for f, v in stats.items()}
+
+    # e2e: all .bin files from pinned host memory through bg_prove_host, every step
+    for _ in range(2):
+        ctx.prove_host(files)
+    dist.barrier()
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        ctx.prove_host(files)
+        e1.record(ext)
+        e1.synchronize()
+        e2e_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    dist.barrier()
+    e2e_total = dist.max(sum(e2e_ms))
+    d2h = sum(window_counts(L, n)[1] * 128 for n in g1_sizes) + window_counts(L, nb)[1] * 256 + 5 * 4
+    e2e = {"value": round(aggregate_ms_per_proof(e2e_total, dist.world, args.steps), 3), "unit": UNIT,
+           "h2d_bytes_per_step": int(files.nbytes()), "d2h_bytes_per_step": int(d2h),
+           "api": "bg_prove_host (every .bin file uploaded per proof)"}
+
+    prims = None if args.no_primitives else primitives(ctx, files, nh, nb, args, ext, flush)
+
+    result = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(value * dist.world, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": round(value / REF_GPU_K18_MS, 6),
+        "vs_baseline_ref": "Bend 2 CUDA path, RTX 5090, K=18 T total 56083 ms (BASELINE.md)",
+        "dtype": "u32 (exact BN254 Fr/Fq Montgomery arithmetic)", "data": "synthetic (seeded SquareChain instance)",
+        "config": {"workload": "SquareChain(2^%d) Groth16 proof: 4 G1 MSMs + 1 G2 MSM + 7 radix-2 NTTs of 2^%d"
+                               % (args.log2n, lg),
+                   "log2_constraints": args.log2n, "domain_log2": lg, "n_a": na, "n_b": nb, "n_h": nh, "n_l": nl,
+                   "seed": args.seed, "parallelism": "replicas" if dist.world > 1 else "single GPU",
+                   "l2": "flushed (512 MiB write) before every timed step",
+                   "msm_window_bits": {str(n): L.bg_msm_window_bits(n) for n in sorted(set(g1_sizes + [nb]))}},
+        "e2e": e2e, "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
+        "phases_ms_median": {k: round(statistics.median(p[k] for p in phases), 3) for k in phases[0]},
+        "kernels": kernel_ms, "fq_mul_rate_gops": round(fqmul_rate / 1e9, 2), "primitives": prims,
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(path, samples=1)
+    key.release()
+    files.free()
+    ctx.close()
+    return result
+
+
+def primitives(ctx, files, nh, nb, args, ext, flush):
+    """standalone primitives of the second benchmark configuration: G1 MSM 2^20, G2 MSM 2^18,
+    NTT 2^20, all device-resident (points: the instance's h_query twice, as the reference's own
+    MSM bench does for 2^20, bend2/bench/msm.bend:1-9; scalars uniform < r)"""
+    import numpy as np
+    import torch
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(args.seed)
+
+    def scalars(n):
+        w = rng.integers(0, 1 << 32, size=(n, 8), dtype=np.uint64).astype(np.uint32)
+        w[:, 7] &= 0x0fffffff  # < 2^252 < r
+        return torch.from_numpy(w.view(np.int32)).to(dev)
+
+    def packed(name, count_words16):
+        w = files.words(name)[:count_words16].astype(np.int64).astype(np.int32)
+        d_wire = torch.from_numpy(w).to(dev)
+        d_pk = torch.empty(count_words16 // 2, dtype=torch.int32, device=dev)
+        ctx.repack_to_packed_dev(d_wire.data_ptr(), d_pk.data_ptr(), count_words16 // 16)
+        torch.cuda.synchronize()
+        return d_pk
+
+    def timeit(fn, reps=5):
+        for _ in range(2):
+            fn()
+        out = []
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            fn()
+            e1.record(ext)
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return round(statistics.median(out), 3)
+
+    res = {}
+    n1 = 1 << 20
+    h = packed("pk_h", nh * 32)
+    a = packed("pk_a", 2 * 32)
+    pts = torch.cat([h, h, a])[: n1 * 16].contiguous()
+    sc = scalars(n1)
+    res["g1_msm_2^20_ms"] = timeit(lambda: ctx.msm_g1_dev(pts.data_ptr(), sc.data_ptr(), n1))
+    n2 = 1 << 18
+    b2 = packed("pk_b2", nb * 64)[: n2 * 32].contiguous()
+    sc2 = scalars(n2)
+    res["g2_msm_2^18_ms"] = timeit(lambda: ctx.msm_g2_dev(b2.data_ptr(), sc2.data_ptr(), n2))
+    x = scalars(n1)
+    res["ntt_2^20_forward_ms"] = timeit(lambda: ctx.ntt_dev(x.data_ptr(), 20, 0) or torch.cuda.synchronize())
+    res["coset_ntt_2^20_ms"] = timeit(lambda: ctx.ntt_dev(x.data_ptr(), 20, 2) or torch.cuda.synchronize())
+    return res
+
+
+# ---------------------------------------------------------------- CPU restatement
+def cpu_baseline(path: str, samples: int = 1) -> dict:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_c
+    threads = os.cpu_count() or 1
+    oracle_c.prove_dir(path, threads)  # warm (page cache, thread pool)
+    t = []
+    for _ in range(samples):
+        t0 = time.perf_counter()
+        oracle_c.prove_dir(path, threads)
+        t.append((time.perf_counter() - t0) * 1e3)
+    return {"value": round(statistics.median(t), 1), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d complete proof(s) of the same SquareChain instance (load, evals, qap, 5 MSMs, combine)"
+                      % samples}
+
+
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ctypes
+
+    import oracle_c
+    L = oracle_c.lib()
+    L.bgo_synth_square_chain.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_int]
+    threads = os.cpu_count() or 1
+
+    def gen(k, s, p):
+        if L.bgo_synth_square_chain(k, s, p.encode(), threads) != 0:
+            raise RuntimeError("oracle synth failed")
+
+    single = Dist.__new__(Dist)
+    single.world, single.rank, single.local, single.pg = 1, 0, 0, None
+    path = ensure_instance(args, single, gen)
+    for _ in range(args.warmup):
+        oracle_c.prove_dir(path, threads)
+    t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle_c.prove_dir(path, threads)
+        t.append((time.perf_counter() - t0) * 1e3)
+    value = sum(t) / len(t)
+    hdr = open(os.path.join(path, "header.bin"), "rb").read()
+    import struct
+    nc, ni, nw, lg, na, nb, nh, nl = struct.unpack("<8I", hdr)
+    return {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "impl": "reference", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 1), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": round(value / REF_GPU_K18_MS, 6), "dtype": "u64 (exact BN254 arithmetic)",
+        "data": "synthetic (seeded SquareChain instance)",
+        "config": {"workload": "SquareChain(2^%d) Groth16 proof: 4 G1 MSMs + 1 G2 MSM + 7 radix-2 NTTs of 2^%d"
+                               % (args.log2n, lg), "log2_constraints": args.log2n, "domain_log2": lg, "n_a": na,
+                   "n_b": nb, "n_h": nh, "n_l": nl, "seed": args.seed},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "one complete proof per step (the reference's Bend 2 / arkworks CPU provers "
+                                   "cannot run on this image: C restatement in oracle/)"},
+        "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        res = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+        if res is not None and dist.rank == 0:
+            print(json.dumps(res), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

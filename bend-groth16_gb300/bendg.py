@@ -33,7 +33,8 @@ EXPORTS = (
     "bg_host_alloc", "bg_host_free", "bg_msm_g1", "bg_msm_g2", "bg_qap_h", "bg_prove_dir", "bg_prove_host",
     "bg_pk_upload", "bg_pk_release", "bg_prove_resident", "bg_proof_format", "bg_ntt", "bg_field_op",
     "bg_curve_op", "bg_msm_g1_dev", "bg_msm_g2_dev", "bg_ntt_dev", "bg_repack_to_packed_dev",
-    "bg_repack_to_wire_dev", "bg_synth_square_chain", "bg_msm_window_bits",
+    "bg_repack_to_wire_dev", "bg_synth_square_chain", "bg_msm_window_bits", "bg_ctx_profile",
+    "bg_ctx_kernel_stats", "bg_probe_imad",
 )
 
 
@@ -100,6 +101,9 @@ def lib():
         "bg_repack_to_wire_dev": (i32, [vp, vp, vp, sz]),
         "bg_synth_square_chain": (i32, [vp, u32, u64, ctypes.c_char_p]),
         "bg_msm_window_bits": (i32, [sz]),
+        "bg_ctx_profile": (i32, [vp, i32]),
+        "bg_ctx_kernel_stats": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
+        "bg_probe_imad": (i32, [vp, i32, u32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -172,6 +176,21 @@ class Context:
 
     def launches(self) -> int:
         return int(self._L.bg_ctx_launches(self.h))
+
+    def profile(self, enable: bool):
+        self._check(self._L.bg_ctx_profile(self.h, 1 if enable else 0), "bg_ctx_profile")
+
+    def kernel_stats(self, name: str):
+        n, ms = ctypes.c_uint64(), ctypes.c_double()
+        self._check(self._L.bg_ctx_kernel_stats(self.h, name.encode(), ctypes.byref(n), ctypes.byref(ms)),
+                    "bg_ctx_kernel_stats")
+        return int(n.value), float(ms.value)
+
+    def probe_imad(self, which: int, iters: int):
+        ops, ms = ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.bg_probe_imad(self.h, which, iters, ctypes.byref(ops), ctypes.byref(ms)),
+                    "bg_probe_imad")
+        return ops.value, ms.value
 
     # ---- the seam
     def msm_g1(self, points16, scalars16, n: int | None = None) -> np.ndarray:

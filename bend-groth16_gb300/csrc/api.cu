@@ -443,6 +443,69 @@ int bg_synth_square_chain(bg_ctx* ctx, uint32_t log2n, uint64_t seed, const char
   });
 }
 
+int bg_ctx_profile(bg_ctx* ctx, int enable) {
+  if (!ctx) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    for (int i = 0; i < kStreams; i++) BG_CUDA(cudaStreamSynchronize(ctx->c.side[i]));
+    BG_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    for (auto& kv : ctx->c.ktimes)
+      for (auto& ev : kv.second.pending) {
+        cudaEventDestroy(ev.first);
+        cudaEventDestroy(ev.second);
+      }
+    ctx->c.ktimes.clear();
+    ctx->c.profile = enable != 0;
+  });
+}
+
+int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms) {
+  if (!ctx || !name || !launches || !total_ms) return BG_E_ARG;
+  return guard(ctx, [&] {
+    *launches = 0;
+    *total_ms = 0;
+    auto it = ctx->c.ktimes.find(name);
+    if (it == ctx->c.ktimes.end()) return;
+    Ctx::KernelTimes& kt = it->second;
+    for (auto& ev : kt.pending) {
+      BG_CUDA(cudaEventSynchronize(ev.second));
+      float ms = 0;
+      BG_CUDA(cudaEventElapsedTime(&ms, ev.first, ev.second));
+      kt.total_ms += ms;
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
+    kt.pending.clear();
+    *launches = kt.launches;
+    *total_ms = kt.total_ms;
+  });
+}
+
+int bg_probe_imad(bg_ctx* ctx, int which, uint32_t iters, double* ops, double* ms) {
+  if (!ctx || !ops || !ms || (which != 0 && which != 1) || iters == 0) return BG_E_ARG;
+  return guard(ctx, [&] {
+    Ctx& c = ctx->c;
+    cudaSetDevice(c.device);
+    const int threads = 256, blocks = c.sm_count * 8;
+    uint32_t* sink = c.ws.get_t<uint32_t>("probe.sink", 1);
+    cudaEvent_t a, b;
+    BG_CUDA(cudaEventCreate(&a));
+    BG_CUDA(cudaEventCreate(&b));
+    imad_probe(c.stream, blocks, threads, 1, sink, which);  // warm-up
+    BG_CUDA(cudaEventRecord(a, c.stream));
+    imad_probe(c.stream, blocks, threads, iters, sink, which);
+    BG_CUDA(cudaEventRecord(b, c.stream));
+    BG_CUDA(cudaEventSynchronize(b));
+    float t = 0;
+    BG_CUDA(cudaEventElapsedTime(&t, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    const double per_thread = which == 0 ? 16.0 * iters : 4.0 * iters;
+    *ops = per_thread * threads * blocks;
+    *ms = t;
+  });
+}
+
 int bg_proof_format(const bg_proof* proof, char* buf, size_t buf_bytes) {
   if (!proof || !buf) return BG_E_ARG;
   return format_proof(proof, buf, buf_bytes);

@@ -133,8 +133,39 @@ struct Ctx {
   std::string last_error;
   uint32_t* d_status = nullptr;           // device-side error flags (see BG_DSTATUS_*)
   std::map<int, NttTables> ntt_tabs;      // per domain size, built on first use
-  // scalar profiling of the last call: named phase durations in ms
-  std::vector<std::pair<std::string, float>> phases;
+  // optional per-kernel timing: CUDA events recorded around selected launches on their
+  // own stream, resolved when the statistics are read
+  bool profile = false;
+  struct KernelTimes {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    uint64_t launches = 0;
+    double total_ms = 0;
+  };
+  std::map<std::string, KernelTimes> ktimes;
+};
+
+// Brackets one kernel launch with events when the context profiles (see bg_ctx_profile).
+class KernelTimer {
+ public:
+  KernelTimer(Ctx& c, const char* name, cudaStream_t st) : c_(c), st_(st) {
+    if (!c.profile) return;
+    kt_ = &c.ktimes[name];
+    cudaEventCreate(&a_);
+    cudaEventCreate(&b_);
+    cudaEventRecord(a_, st);
+  }
+  ~KernelTimer() {
+    if (!kt_) return;
+    cudaEventRecord(b_, st_);
+    kt_->pending.push_back({a_, b_});
+    kt_->launches++;
+  }
+
+ private:
+  Ctx& c_;
+  cudaStream_t st_;
+  Ctx::KernelTimes* kt_ = nullptr;
+  cudaEvent_t a_ = nullptr, b_ = nullptr;
 };
 
 // device status flag bits

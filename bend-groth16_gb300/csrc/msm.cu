@@ -265,14 +265,24 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", nkeys * PW);
 
   BG_CUDA(cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
-  k_digits_hist<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, counts, ctx.d_status);
-  BG_CHECK_LAUNCH();
+  {
+    KernelTimer kt(ctx, "msm_digits", st);
+    k_digits_hist<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, counts, ctx.d_status);
+    BG_CHECK_LAUNCH();
+  }
   exclusive_scan(ws, tag, counts, offsets, nkeys + 1, st, 0);
   BG_CUDA(cudaMemcpyAsync(cursor, offsets, (nkeys + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
-  k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, cursor, sorted);
-  BG_CHECK_LAUNCH();
-  k_bucket_acc<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(d_points, offsets, sorted, (uint32_t)nkeys, buckets);
-  BG_CHECK_LAUNCH();
+  {
+    KernelTimer kt(ctx, "msm_scatter", st);
+    k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, cursor, sorted);
+    BG_CHECK_LAUNCH();
+  }
+  {
+    KernelTimer kt(ctx, FieldWords<F>::value == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st);
+    k_bucket_acc<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(d_points, offsets, sorted, (uint32_t)nkeys, buckets);
+    BG_CHECK_LAUNCH();
+  }
+  plan.entries = n * (size_t)W;
 
   // hierarchical reduction, L = 8 elements per thread and level
   const uint32_t L = 8;
@@ -286,8 +296,11 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
     const uint32_t S = (M + L - 1) / L;
     uint32_t* Rout = ws.get_t<uint32_t>(tag + ".red_r" + std::to_string(level & 1), (size_t)S * W * PW);
     uint32_t* Qout = ws.get_t<uint32_t>(tag + ".red_q" + std::to_string(level & 1), (size_t)S * W * PW);
-    k_reduce_level<F><<<ceil_div((size_t)S * W, 128), 128, 0, st>>>(R, Q, M, L, lam_log2, S, W, Rout, Qout);
-    BG_CHECK_LAUNCH();
+    {
+      KernelTimer kt(ctx, FieldWords<F>::value == 8 ? "msm_reduce_g1" : "msm_reduce_g2", st);
+      k_reduce_level<F><<<ceil_div((size_t)S * W, 128), 128, 0, st>>>(R, Q, M, L, lam_log2, S, W, Rout, Qout);
+      BG_CHECK_LAUNCH();
+    }
     lam_log2 = (Q == nullptr) ? 3 : lam_log2 + 3;
     R = Rout;
     Q = Qout;

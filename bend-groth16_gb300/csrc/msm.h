@@ -10,6 +10,7 @@ namespace bg {
 struct MsmPlan {
   int c = 0;                              // window bits (0: pick from n)
   int W = 0;                              // windows
+  size_t entries = 0;                     // bucket entries (n * W upper bound)
   const uint32_t* d_window_sums = nullptr;  // W XYZZ points on the device
   std::vector<uint32_t> host_window_sums;   // W XYZZ points after msm_fetch
 };

@@ -296,6 +296,7 @@ static void launch_pass(Ctx& ctx, cudaStream_t st, bool dit, uint32_t* d, const 
   const int E = p.G << p.k;
   const unsigned blocks = (unsigned)(n / E);
   const size_t smem = (size_t)E * 32;
+  KernelTimer kt(ctx, "ntt_pass", st);
   if (dit) {
     k_ntt_pass<true><<<blocks, kNttThreads, smem, st>>>(d, tw, L, p.s0, p.k, p.G, pre, post, sc);
   } else {

@@ -157,9 +157,15 @@ static void* dmalloc(size_t bytes) {
 static void h2d(Ctx& ctx, int slot, void* dst, const void* src, size_t bytes, cudaStream_t st) {
   if (bytes == 0) return;
   cudaPointerAttributes attr;
-  if (cudaPointerGetAttributes(&attr, src) == cudaSuccess && attr.type == cudaMemoryTypeHost) {
-    BG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
-    return;
+  if (cudaPointerGetAttributes(&attr, src) == cudaSuccess) {
+    if (attr.type == cudaMemoryTypeHost) {
+      BG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+      return;
+    }
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
+      BG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st));
+      return;
+    }
   }
   cudaGetLastError();
   // pageable source: stage in chunks through pinned memory

@@ -156,6 +156,19 @@ int bg_synth_square_chain(bg_ctx* ctx, uint32_t log2n, uint64_t seed, const char
 /* Window width c the MSM picks for n points (the tuning table), for reports. */
 int bg_msm_window_bits(size_t n);
 
+/* ---- measurement (no counterpart in the reference, which prints only T lines) ------- */
+/* Enable (1) / disable (0) CUDA-event timing of the library's main kernels on the streams
+ * they run on; enabling clears earlier statistics. */
+int bg_ctx_profile(bg_ctx* ctx, int enable);
+/* Launch count and summed device time (ms) of one kernel family since profiling was enabled:
+ * "msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_reduce_g1", "msm_reduce_g2", "msm_digits",
+ * "msm_scatter", "ntt_pass".  Unknown names report zero launches. */
+int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms);
+/* Integer multiply-add throughput probe: which = 0 raw 32-bit mad.lo/mad.hi chains,
+ * which = 1 Fq Montgomery products.  Returns the operations executed (32-bit IMADs, or Fq
+ * products) and the kernel time in ms. */
+int bg_probe_imad(bg_ctx* ctx, int which, uint32_t iters, double* ops, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,17 +46,21 @@ def test_ntt_full_size_properties(ctx, lg):
     w[:, 15] &= 0x0fff
     xw = w.reshape(-1)
     fwd = ctx.ntt(xw, lg, bendg.NTT_FORWARD)
+    import oracle_c
+    assert np.array_equal(fwd, oracle_c.ntt(xw, lg, bendg.NTT_FORWARD))
     assert np.array_equal(ctx.ntt(fwd, lg, bendg.NTT_INVERSE), xw)
     cf = ctx.ntt(xw, lg, bendg.NTT_COSET_FORWARD)
     assert np.array_equal(ctx.ntt(cf, lg, bendg.NTT_COSET_INVERSE), xw)
-    # evaluation identities at a few indexes: y_j = sum_i x_i w^(ij), coset: sum_i x_i (g w^j)^i
-    x = fr_from_wire_mont(xw)
-    y = fr_from_wire_mont(fwd[: 16 * 4])
-    yc = fr_from_wire_mont(cf[: 16 * 4])
-    w1 = o.omega(lg)
-    for j in (0, 1, 3):
-        assert y[j] == o.poly_eval(x, pow(w1, j, o.P_FR))
-        assert yc[j] == o.poly_eval(x, o.GEN * pow(w1, j, o.P_FR) % o.P_FR)
+    assert np.array_equal(cf, oracle_c.ntt(xw, lg, bendg.NTT_COSET_FORWARD))
+    if lg == 19:
+        # evaluation identities at a few indexes: y_j = sum_i x_i w^(ij), coset: sum_i x_i (g w^j)^i
+        x = fr_from_wire_mont(xw)
+        y = fr_from_wire_mont(fwd[: 16 * 4])
+        yc = fr_from_wire_mont(cf[: 16 * 4])
+        w1 = o.omega(lg)
+        for j in (0, 1, 3):
+            assert y[j] == o.poly_eval(x, pow(w1, j, o.P_FR))
+            assert yc[j] == o.poly_eval(x, o.GEN * pow(w1, j, o.P_FR) % o.P_FR)
 
 
 @pytest.mark.parametrize("k", [4, 10])
@@ -81,8 +85,10 @@ def test_qap_h_random_vs_oracle(ctx, lg):
     assert fr_from_wire_mont(h) == want and want[-1] == 0
 
 
-def test_qap_h_full_size_identity(ctx):
-    """d = 2^21 (the K=20 domain): A(x) B(x) - C(x) = h(x) (x^d - 1) at a random point"""
+def test_qap_h_full_size_vs_c_oracle(ctx):
+    """d = 2^21 (the K=20 domain), c = a*b on the domain: h equals the C oracle's bit for bit
+    and its top coefficient is 0"""
+    import oracle_c
     lg = 21
     n = 1 << lg
     rng = np.random.default_rng(5)
@@ -90,14 +96,7 @@ def test_qap_h_full_size_identity(ctx):
     b = rng.integers(0, 1 << 16, size=(n, 16), dtype=np.uint32)
     a[:, 15] &= 0x0fff
     b[:, 15] &= 0x0fff
-    ai, bi = fr_from_wire_mont(a), fr_from_wire_mont(b)
-    ci = [x * y % o.P_FR for x, y in zip(ai, bi)]
-    cw = fr_wire_mont(ci)
-    h = fr_from_wire_mont(ctx.qap_h(a.reshape(-1), b.reshape(-1), cw.reshape(-1), lg))
-    assert h[-1] == 0
-    pa = fr_from_wire_mont(ctx.ntt(a.reshape(-1), lg, bendg.NTT_INVERSE))
-    pb = fr_from_wire_mont(ctx.ntt(b.reshape(-1), lg, bendg.NTT_INVERSE))
-    pc = fr_from_wire_mont(ctx.ntt(cw.reshape(-1), lg, bendg.NTT_INVERSE))
-    x = 0x1234567890ABCDEF1234567890ABCDEF
-    lhs = (o.poly_eval(pa, x) * o.poly_eval(pb, x) - o.poly_eval(pc, x)) % o.P_FR
-    assert lhs == o.poly_eval(h, x) * (pow(x, n, o.P_FR) - 1) % o.P_FR
+    c = ctx.field_op(bendg.FIELD_FR, bendg.FOP_MUL, a, b)
+    h = ctx.qap_h(a.reshape(-1), b.reshape(-1), c, lg)
+    assert np.array_equal(h, oracle_c.qap_h(a.reshape(-1), b.reshape(-1), c, lg))
+    assert not h[-16:].any()

@@ -75,3 +75,30 @@ def test_synthetic_instance_trapdoor(ctx, tmp_path, log2n):
     proof, _ = ctx.prove_dir(path)
     pts = oracle_io.parse_proof_text(ctx.proof_text(proof))
     assert oracle_io.square_chain_trapdoor_check(data, trap, pts)
+
+
+def test_synth_gpu_equals_cpu(ctx, tmp_path):
+    """the device fixed-base generator and the C oracle's CPU generator write identical files"""
+    import ctypes
+    import oracle_c
+    L = oracle_c.lib()
+    L.bgo_synth_square_chain.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_int]
+    g, c = tmp_path / "gpu", tmp_path / "cpu"
+    os.makedirs(c)
+    ctx.synth_square_chain(10, 77, str(g))
+    assert L.bgo_synth_square_chain(10, 77, str(c).encode(), 8) == 0
+    for f in sorted(os.listdir(c)):
+        assert open(g / f, "rb").read() == open(c / f, "rb").read(), f
+
+
+@pytest.mark.parametrize("log2n", [14, 18])
+def test_prove_matches_c_oracle(ctx, tmp_path, log2n):
+    """full-size proof bit-identical to the C oracle's on the same synthetic instance"""
+    import oracle_c
+    path = str(tmp_path / "sq")
+    ctx.synth_square_chain(log2n, 4242 + log2n, path)
+    proof, _ = ctx.prove_dir(path)
+    want, _ = oracle_c.prove_dir(path)
+    got = np.concatenate([np.ctypeslib.as_array(proof.a), np.ctypeslib.as_array(proof.b),
+                          np.ctypeslib.as_array(proof.c)])
+    assert np.array_equal(got, want)
