@@ -104,6 +104,19 @@ class PinnedBuf {
   size_t cap_ = 0;
 };
 
+// Pinned host buffers cached by name (allocation synchronises the device, so it happens once)
+class PinnedCache {
+ public:
+  template <class T>
+  T* get_t(const std::string& name, size_t count) {
+    auto& b = bufs_[name];
+    return static_cast<T*>(b.get(count * sizeof(T)));
+  }
+
+ private:
+  std::map<std::string, PinnedBuf> bufs_;
+};
+
 constexpr int kStreams = 6;
 
 // NTT tables for one domain size 2^L (device pointers into the context workspace)
@@ -130,6 +143,7 @@ struct Ctx {
   cudaEvent_t ev_join[kStreams] = {};
   Workspace ws;
   PinnedBuf pinned[4];
+  PinnedCache host_cache;
   std::string last_error;
   uint32_t* d_status = nullptr;           // device-side error flags (see BG_DSTATUS_*)
   std::map<int, NttTables> ntt_tabs;      // per domain size, built on first use
@@ -142,6 +156,16 @@ struct Ctx {
     double total_ms = 0;
   };
   std::map<std::string, KernelTimes> ktimes;
+  // named events for cross-stream ordering, created on first use
+  std::map<std::string, cudaEvent_t> events;
+  cudaEvent_t event(const std::string& name) {
+    auto it = events.find(name);
+    if (it != events.end()) return it->second;
+    cudaEvent_t e = nullptr;
+    BG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    events[name] = e;
+    return e;
+  }
 };
 
 // Brackets one kernel launch with events when the context profiles (see bg_ctx_profile).

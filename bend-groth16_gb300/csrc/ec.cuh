@@ -16,6 +16,19 @@
 
 namespace bg {
 
+// products used by the curve formulas: out of line (see mul_ool)
+BG_DEV Fq fmul(const Fq& a, const Fq& b) { return mul_ool(a, b); }
+BG_DEV Fq fsqr(const Fq& a) { return mul_ool(a, a); }
+BG_DEV Fq2 fmul(const Fq2& a, const Fq2& b) {
+  const Fq t0 = mul_ool(a.c0, b.c0);
+  const Fq t1 = mul_ool(a.c1, b.c1);
+  const Fq t2 = mul_ool(add(a.c0, a.c1), add(b.c0, b.c1));
+  return {sub(t0, t1), sub(sub(t2, t0), t1)};
+}
+BG_DEV Fq2 fsqr(const Fq2& a) {
+  return {mul_ool(add(a.c0, a.c1), sub(a.c0, a.c1)), mul_ool(dbl(a.c0), a.c1)};
+}
+
 template <class F>
 struct Affine {
   F x, y;
@@ -72,14 +85,14 @@ BG_DEV XYZZ<F> xyzz_neg(const XYZZ<F>& p) {
 template <class F>
 BG_DEV XYZZ<F> xyzz_dbl_affine(const Affine<F>& p) {
   const F u = dbl(p.y);
-  const F v = sqr(u);
-  const F w = mul(u, v);
-  const F s = mul(p.x, v);
-  const F x2 = sqr(p.x);
+  const F v = fsqr(u);
+  const F w = fmul(u, v);
+  const F s = fmul(p.x, v);
+  const F x2 = fsqr(p.x);
   const F m = add(dbl(x2), x2);
   XYZZ<F> r;
-  r.x = sub(sqr(m), dbl(s));
-  r.y = sub(mul(m, sub(s, r.x)), mul(w, p.y));
+  r.x = sub(fsqr(m), dbl(s));
+  r.y = sub(fmul(m, sub(s, r.x)), fmul(w, p.y));
   r.zz = v;
   r.zzz = w;
   return r;
@@ -90,16 +103,16 @@ template <class F>
 BG_DEV XYZZ<F> xyzz_dbl(const XYZZ<F>& p) {
   if (is_inf(p)) return p;
   const F u = dbl(p.y);
-  const F v = sqr(u);
-  const F w = mul(u, v);
-  const F s = mul(p.x, v);
-  const F x2 = sqr(p.x);
+  const F v = fsqr(u);
+  const F w = fmul(u, v);
+  const F s = fmul(p.x, v);
+  const F x2 = fsqr(p.x);
   const F m = add(dbl(x2), x2);
   XYZZ<F> r;
-  r.x = sub(sqr(m), dbl(s));
-  r.y = sub(mul(m, sub(s, r.x)), mul(w, p.y));
-  r.zz = mul(v, p.zz);
-  r.zzz = mul(w, p.zzz);
+  r.x = sub(fsqr(m), dbl(s));
+  r.y = sub(fmul(m, sub(s, r.x)), fmul(w, p.y));
+  r.zz = fmul(v, p.zz);
+  r.zzz = fmul(w, p.zzz);
   return r;
 }
 
@@ -108,22 +121,22 @@ template <class F>
 BG_DEV XYZZ<F> xyzz_madd(const XYZZ<F>& p, const Affine<F>& q) {
   if (is_inf(q)) return p;
   if (is_inf(p)) return xyzz_from_affine(q);
-  const F u2 = mul(q.x, p.zz);
-  const F s2 = mul(q.y, p.zzz);
+  const F u2 = fmul(q.x, p.zz);
+  const F s2 = fmul(q.y, p.zzz);
   const F pp_ = sub(u2, p.x);
   const F r_ = sub(s2, p.y);
   if (is_zero(pp_)) {
     if (is_zero(r_)) return xyzz_dbl_affine(q);
     return xyzz_inf<F>();
   }
-  const F pp = sqr(pp_);
-  const F ppp = mul(pp_, pp);
-  const F qq = mul(p.x, pp);
+  const F pp = fsqr(pp_);
+  const F ppp = fmul(pp_, pp);
+  const F qq = fmul(p.x, pp);
   XYZZ<F> r;
-  r.x = sub(sub(sqr(r_), ppp), dbl(qq));
-  r.y = sub(mul(r_, sub(qq, r.x)), mul(p.y, ppp));
-  r.zz = mul(p.zz, pp);
-  r.zzz = mul(p.zzz, ppp);
+  r.x = sub(sub(fsqr(r_), ppp), dbl(qq));
+  r.y = sub(fmul(r_, sub(qq, r.x)), fmul(p.y, ppp));
+  r.zz = fmul(p.zz, pp);
+  r.zzz = fmul(p.zzz, ppp);
   return r;
 }
 
@@ -132,24 +145,24 @@ template <class F>
 BG_DEV XYZZ<F> xyzz_add(const XYZZ<F>& p, const XYZZ<F>& q) {
   if (is_inf(q)) return p;
   if (is_inf(p)) return q;
-  const F u1 = mul(p.x, q.zz);
-  const F u2 = mul(q.x, p.zz);
-  const F s1 = mul(p.y, q.zzz);
-  const F s2 = mul(q.y, p.zzz);
+  const F u1 = fmul(p.x, q.zz);
+  const F u2 = fmul(q.x, p.zz);
+  const F s1 = fmul(p.y, q.zzz);
+  const F s2 = fmul(q.y, p.zzz);
   const F pp_ = sub(u2, u1);
   const F r_ = sub(s2, s1);
   if (is_zero(pp_)) {
     if (is_zero(r_)) return xyzz_dbl(p);
     return xyzz_inf<F>();
   }
-  const F pp = sqr(pp_);
-  const F ppp = mul(pp_, pp);
-  const F qq = mul(u1, pp);
+  const F pp = fsqr(pp_);
+  const F ppp = fmul(pp_, pp);
+  const F qq = fmul(u1, pp);
   XYZZ<F> r;
-  r.x = sub(sub(sqr(r_), ppp), dbl(qq));
-  r.y = sub(mul(r_, sub(qq, r.x)), mul(s1, ppp));
-  r.zz = mul(mul(p.zz, q.zz), pp);
-  r.zzz = mul(mul(p.zzz, q.zzz), ppp);
+  r.x = sub(sub(fsqr(r_), ppp), dbl(qq));
+  r.y = sub(fmul(r_, sub(qq, r.x)), fmul(s1, ppp));
+  r.zz = fmul(fmul(p.zz, q.zz), pp);
+  r.zzz = fmul(fmul(p.zzz, q.zzz), ppp);
   return r;
 }
 

@@ -11,10 +11,11 @@
 //                     histogram of (window, |d|-1) bucket keys
 //   2. exclusive scan of the histogram -> bucket offsets
 //   3. k_scatter      (point index | sign << 31) written into bucket order
-//   4. k_bucket_acc   one thread per bucket: XYZZ accumulator += +-P (mixed add)
-//   5. k_reduce_level hierarchical running sums: sum_b (b+1) B_b per window, segments of
-//                     L buckets per thread, log_L(2^(c-1)) levels
-//   6. host: W window sums -> Horner with c doublings per window -> affine.
+//   4. k_bucket_acc   load-balanced slices of K entries per thread: XYZZ accumulator += +-P
+//                     (mixed add); k_bucket_fixup joins buckets cut by slice boundaries
+//   5. k_window_reduce one CTA per window part: running sums over 16 buckets per thread, an
+//                     in-CTA suffix scan and tree sum give sum_b (b+1) B_b for the part
+//   6. host: parts -> window sums -> Horner with c doublings per window -> affine.
 // Window sums and the final point are exact group elements, so the affine result equals the
 // reference's for the same inputs regardless of bucket order inside a window.
 #include "common.cuh"
@@ -161,62 +162,135 @@ __global__ void k_scatter(const uint32_t* __restrict__ scalars, size_t n, int c,
   }
 }
 
+
 // ---------------------------------------------------------------- buckets
+// Segmented accumulation: the bucket-ordered entry list (T entries) is cut into slices of K
+// entries, one per thread, so every thread runs exactly K mixed additions whatever the bucket
+// sizes are (one thread per bucket would idle most lanes of a warp on Poisson-sized buckets).
+// A run of entries that covers a whole bucket is written to that bucket; a run cut by a slice
+// boundary is written to the thread's slot 0 (run started in an earlier slice) or slot 1
+// (run continues into a later slice), and k_bucket_fixup sums the pieces.
 template <class F>
 __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__ points,
                                                     const uint32_t* __restrict__ offsets,
                                                     const uint32_t* __restrict__ sorted, uint32_t nbuckets,
-                                                    uint32_t* __restrict__ buckets) {
+                                                    uint32_t K, uint32_t* __restrict__ buckets,
+                                                    uint32_t* __restrict__ slot0, uint32_t* __restrict__ slot1) {
   constexpr int FW = FieldWords<F>::value;
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= nbuckets) return;
-  const uint32_t beg = offsets[g], end = offsets[g + 1];
+  constexpr int PW = 4 * FW;
+  const uint32_t total = offsets[nbuckets];
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t beg64 = (uint64_t)t * K;
+  if (beg64 >= total) return;
+  const uint32_t beg = (uint32_t)beg64;
+  const uint32_t end = (total - beg) < K ? total : beg + K;
+  // bucket holding entry `beg`: the last b with offsets[b] <= beg
+  uint32_t lo = 0, hi = nbuckets;  // offsets[lo] <= beg < offsets[hi]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (offsets[mid] <= beg) lo = mid;
+    else hi = mid;
+  }
+  // One flat loop of exactly (end - beg) mixed additions, so the lanes of a warp stay in
+  // step; a bucket boundary only costs a short divergent flush.
+  uint32_t b = lo;
+  uint32_t bstart = offsets[b], bend = offsets[b + 1];
   XYZZ<F> acc = xyzz_inf<F>();
   for (uint32_t e = beg; e < end; e++) {
     const uint32_t code = sorted[e];
     Affine<F> p = load_affine<F>(points + (size_t)(code & 0x7fffffffu) * 2 * FW);
     if (code >> 31) p = affine_neg(p);
     acc = xyzz_madd(acc, p);
+    if (e + 1 == bend || e + 1 == end) {
+      uint32_t* dst = (bstart < beg) ? slot0 + (size_t)t * PW
+                      : (bend > end) ? slot1 + (size_t)t * PW
+                                     : buckets + (size_t)b * PW;
+      store_xyzz(dst, acc);
+      acc = xyzz_inf<F>();
+      if (e + 1 < end) {
+        do {
+          b++;
+        } while (offsets[b + 1] <= e + 1);  // skip empty buckets
+        bstart = offsets[b];
+        bend = offsets[b + 1];
+      }
+    }
   }
-  store_xyzz(buckets + (size_t)g * 4 * FW, acc);
 }
 
-// One level of the bucket reduction.  Input per window: M pairs (R_e, Q_e) representing
-// sum_e [Q_e + lam * e * R_e] (level 1: Q absent, R = buckets, weights b + 1).  Thread (w, u)
-// folds elements [uL, uL + L) into R'_u = sum R_e and
-// Q'_u = sum Q_e + lam * sum_e (e - uL) R_e   (level 1: Q'_u = sum_k (k + 1) B_{uL+k}),
-// so the window sum is sum_u [Q'_u + (lam L) u R'_u].  One segment left => window sum = Q'_0.
+// One thread per bucket: empty buckets become infinity; a bucket cut by slice boundaries is
+// the sum of slot1 of its first slice and slot0 of every later slice it reaches.
 template <class F>
-__global__ void __launch_bounds__(128) k_reduce_level(const uint32_t* __restrict__ R, const uint32_t* __restrict__ Q,
-                                                      uint32_t M, uint32_t L, int lam_log2, uint32_t S,
-                                                      uint32_t W, uint32_t* __restrict__ Rout,
-                                                      uint32_t* __restrict__ Qout) {
-  constexpr int FW = FieldWords<F>::value;
-  constexpr int PW = 4 * FW;
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S * W) return;
-  const uint32_t w = t / S, u = t % S;
-  const uint32_t beg = u * L;
-  const uint32_t len = (M - beg) < L ? (M - beg) : L;
-  const uint32_t* Rw = R + ((size_t)w * M + beg) * PW;
-  XYZZ<F> run = xyzz_inf<F>(), acc = xyzz_inf<F>();
-  if (Q == nullptr) {
-    for (int k = (int)len - 1; k >= 0; k--) {
-      run = xyzz_add(run, load_xyzz<F>(Rw + (size_t)k * PW));
-      acc = xyzz_add(acc, run);
-    }
-  } else {
-    for (int k = (int)len - 1; k >= 1; k--) {
-      run = xyzz_add(run, load_xyzz<F>(Rw + (size_t)k * PW));
-      acc = xyzz_add(acc, run);
-    }
-    run = xyzz_add(run, load_xyzz<F>(Rw));
-    for (int d = 0; d < lam_log2; d++) acc = xyzz_dbl(acc);
-    const uint32_t* Qw = Q + ((size_t)w * M + beg) * PW;
-    for (uint32_t k = 0; k < len; k++) acc = xyzz_add(acc, load_xyzz<F>(Qw + (size_t)k * PW));
+__global__ void __launch_bounds__(128) k_bucket_fixup(const uint32_t* __restrict__ offsets, uint32_t nbuckets,
+                                                      uint32_t K, const uint32_t* __restrict__ slot0,
+                                                      const uint32_t* __restrict__ slot1,
+                                                      uint32_t* __restrict__ buckets) {
+  constexpr int PW = 4 * FieldWords<F>::value;
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbuckets) return;
+  const uint32_t s = offsets[b], e = offsets[b + 1];
+  if (s == e) {
+    store_xyzz(buckets + (size_t)b * PW, xyzz_inf<F>());
+    return;
   }
-  store_xyzz(Rout + (size_t)t * PW, run);
-  store_xyzz(Qout + (size_t)t * PW, acc);
+  const uint32_t tf = s / K, tl = (e - 1) / K;
+  if (tf == tl) return;  // written whole by k_bucket_acc
+  XYZZ<F> acc = load_xyzz<F>(slot1 + (size_t)tf * PW);
+  for (uint32_t t = tf + 1; t <= tl; t++) acc = xyzz_add(acc, load_xyzz<F>(slot0 + (size_t)t * PW));
+  store_xyzz(buckets + (size_t)b * PW, acc);
+}
+
+// Window reduction, one CTA per (window, part).  Part j of window w covers buckets
+// [j RT M, (j+1) RT M); thread t folds M consecutive buckets into R_t = sum B and
+// T_t = sum_k (k+1) B_{tM+k} (running sums).  The part's weighted sum
+//   S_j = sum_{local b} (b+1) B_b = sum_t T_t + M sum_{t>=1} Suf_t,   Suf_t = sum_{t'>=t} R_t'
+// comes from an in-CTA suffix scan of R and a tree sum; the part also reports R_j = Suf_0.
+// The host finishes window w as sum_j S_j + (RT M) sum_j j R_j.
+template <class F>
+__global__ void k_window_reduce(const uint32_t* __restrict__ buckets, uint32_t nb, uint32_t M, uint32_t J,
+                                uint32_t* __restrict__ out) {
+  constexpr int PW = 4 * FieldWords<F>::value;
+  extern __shared__ uint32_t sm[];
+  const uint32_t RT = blockDim.x;
+  const uint32_t w = blockIdx.x / J, j = blockIdx.x % J, t = threadIdx.x;
+  const uint32_t* B = buckets + ((size_t)w * nb + ((size_t)j * RT + t) * M) * PW;
+  XYZZ<F> run = xyzz_inf<F>(), acc = xyzz_inf<F>();
+  for (int k = (int)M - 1; k >= 0; k--) {
+    run = xyzz_add(run, load_xyzz<F>(B + (size_t)k * PW));
+    acc = xyzz_add(acc, run);
+  }
+  // inclusive suffix scan of R over the CTA (Hillis-Steele)
+  store_xyzz(sm + (size_t)t * PW, run);
+  __syncthreads();
+  for (uint32_t d = 1; d < RT; d <<= 1) {
+    XYZZ<F> v = xyzz_inf<F>();
+    if (t + d < RT) v = load_xyzz<F>(sm + (size_t)(t + d) * PW);
+    __syncthreads();
+    run = xyzz_add(run, v);
+    store_xyzz(sm + (size_t)t * PW, run);
+    __syncthreads();
+  }
+  XYZZ<F> total_r;
+  if (t == 0) total_r = run;
+  // Y_t = T_t + M Suf_t (t >= 1), Y_0 = T_0
+  if (t >= 1) {
+    for (uint32_t m = M; m > 1; m >>= 1) run = xyzz_dbl(run);
+    acc = xyzz_add(acc, run);
+  }
+  __syncthreads();
+  store_xyzz(sm + (size_t)t * PW, acc);
+  __syncthreads();
+  for (uint32_t d = RT >> 1; d >= 1; d >>= 1) {
+    if (t < d) {
+      acc = xyzz_add(acc, load_xyzz<F>(sm + (size_t)(t + d) * PW));
+      store_xyzz(sm + (size_t)t * PW, acc);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    store_xyzz(out + (size_t)blockIdx.x * 2 * PW, acc);
+    store_xyzz(out + ((size_t)blockIdx.x * 2 + 1) * PW, total_r);
+  }
 }
 
 // ---------------------------------------------------------------- host driver
@@ -240,9 +314,13 @@ struct HostField<Fq2> {
   typedef bgh::Fq2Ops T;
 };
 
+// entries per accumulation thread
+template <class F>
+constexpr uint32_t kSlice = FieldWords<F>::value == 8 ? 32 : 16;
+
 template <class F>
 void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
-                const uint32_t* d_scalars, size_t n, MsmPlan& plan) {
+                const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce) {
   constexpr int FW = FieldWords<F>::value;
   constexpr int PW = 4 * FW;
   if (n == 0) {
@@ -250,19 +328,25 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
     return;
   }
   if (n >= 0x80000000ull) throw Error(BG_E_ARG, "msm: n must be below 2^31");
+  msm_init_kernels();
   const int c = plan.c > 0 ? plan.c : msm_pick_c(n);
   const int W = 254 / c + 1;
   const uint32_t nb = 1u << (c - 1);
   const size_t nkeys = (size_t)W * nb;
   plan.c = c;
   plan.W = W;
+  const uint32_t K = kSlice<F>;
+  const size_t max_entries = n * (size_t)W;
+  const size_t max_threads = (max_entries + K - 1) / K;
 
   Workspace& ws = ctx.ws;
   uint32_t* counts = ws.get_t<uint32_t>(tag + ".counts", nkeys + 1);
   uint32_t* offsets = ws.get_t<uint32_t>(tag + ".offsets", nkeys + 1);
   uint32_t* cursor = ws.get_t<uint32_t>(tag + ".cursor", nkeys + 1);
-  uint32_t* sorted = ws.get_t<uint32_t>(tag + ".sorted", n * (size_t)W);
+  uint32_t* sorted = ws.get_t<uint32_t>(tag + ".sorted", max_entries);
   uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", nkeys * PW);
+  uint32_t* slot0 = ws.get_t<uint32_t>(tag + ".slot0", max_threads * PW);
+  uint32_t* slot1 = ws.get_t<uint32_t>(tag + ".slot1", max_threads * PW);
 
   BG_CUDA(cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
   {
@@ -278,50 +362,53 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
     BG_CHECK_LAUNCH();
   }
   {
-    KernelTimer kt(ctx, FieldWords<F>::value == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st);
-    k_bucket_acc<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(d_points, offsets, sorted, (uint32_t)nkeys, buckets);
+    KernelTimer kt(ctx, FW == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st);
+    k_bucket_acc<F><<<ceil_div(max_threads, 128), 128, 0, st>>>(d_points, offsets, sorted, (uint32_t)nkeys, K,
+                                                                buckets, slot0, slot1);
     BG_CHECK_LAUNCH();
   }
-  plan.entries = n * (size_t)W;
-
-  // hierarchical reduction, L = 8 elements per thread and level
-  const uint32_t L = 8;
-  uint32_t M = nb;
-  const uint32_t* R = buckets;
-  const uint32_t* Q = nullptr;
-  int lam_log2 = 0;
-  int level = 0;
-  uint32_t* out_q = nullptr;
-  while (true) {
-    const uint32_t S = (M + L - 1) / L;
-    uint32_t* Rout = ws.get_t<uint32_t>(tag + ".red_r" + std::to_string(level & 1), (size_t)S * W * PW);
-    uint32_t* Qout = ws.get_t<uint32_t>(tag + ".red_q" + std::to_string(level & 1), (size_t)S * W * PW);
-    {
-      KernelTimer kt(ctx, FieldWords<F>::value == 8 ? "msm_reduce_g1" : "msm_reduce_g2", st);
-      k_reduce_level<F><<<ceil_div((size_t)S * W, 128), 128, 0, st>>>(R, Q, M, L, lam_log2, S, W, Rout, Qout);
-      BG_CHECK_LAUNCH();
-    }
-    lam_log2 = (Q == nullptr) ? 3 : lam_log2 + 3;
-    R = Rout;
-    Q = Qout;
-    out_q = Qout;
-    M = S;
-    level++;
-    if (S == 1) break;
+  {
+    KernelTimer kt(ctx, FW == 8 ? "msm_fixup_g1" : "msm_fixup_g2", st);
+    k_bucket_fixup<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(offsets, (uint32_t)nkeys, K, slot0, slot1, buckets);
+    BG_CHECK_LAUNCH();
   }
-  plan.d_window_sums = out_q;
-  plan.host_window_sums.resize((size_t)W * PW);
+  plan.entries = max_entries;
+
+  // window reduction: RT threads x M buckets x J parts per window
+  const uint32_t RT = nb < 256 ? nb : 256;
+  const uint32_t M = (nb / RT) < 16 ? nb / RT : 16;
+  const uint32_t J = nb / (RT * M);
+  uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)W * J * 2 * PW);
+  cudaStream_t rs = st;
+  if (st_reduce && st_reduce != st) {
+    // the latency-bound reduction runs on its own stream and overlaps whatever `st` does next
+    cudaEvent_t ev = ctx.event(tag + ".acc_done");
+    BG_CUDA(cudaEventRecord(ev, st));
+    BG_CUDA(cudaStreamWaitEvent(st_reduce, ev, 0));
+    rs = st_reduce;
+  }
+  {
+    KernelTimer kt(ctx, FW == 8 ? "msm_reduce_g1" : "msm_reduce_g2", rs);
+    k_window_reduce<F><<<W * J, RT, RT * PW * sizeof(uint32_t), rs>>>(buckets, nb, M, J, parts);
+    BG_CHECK_LAUNCH();
+  }
+  plan.fetch_stream = rs;
+  plan.J = J;
+  plan.part_span = RT * M;
+  plan.d_window_sums = parts;
+  plan.host_window_sums = ctx.host_cache.get_t<uint32_t>(tag + ".window_sums", (size_t)W * J * 2 * PW);
 }
 
 template <class F>
 void msm_fetch(cudaStream_t st, MsmPlan& plan) {
   constexpr int PW = 4 * FieldWords<F>::value;
   if (plan.W == 0) return;
-  BG_CUDA(cudaMemcpyAsync(plan.host_window_sums.data(), plan.d_window_sums, (size_t)plan.W * PW * sizeof(uint32_t),
-                          cudaMemcpyDeviceToHost, st));
+  if (plan.fetch_stream) st = plan.fetch_stream;
+  BG_CUDA(cudaMemcpyAsync(plan.host_window_sums, plan.d_window_sums,
+                          (size_t)plan.W * plan.J * 2 * PW * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
 }
 
-// sum_w 2^(c w) S_w on the host (Horner, c doublings per window)
+// Window w = sum_j S_j + span * sum_j j R_j; total = sum_w 2^(c w) window_w (Horner).
 template <class F>
 void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32) {
   typedef typename HostField<F>::T H;
@@ -329,15 +416,33 @@ void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32) {
   bgh::Xyzz<H> acc = bgh::xyzz_inf<H>();
   for (int w = plan.W - 1; w >= 0; w--) {
     for (int d = 0; d < plan.c; d++) acc = bgh::xyzz_dbl(acc);
-    acc = bgh::xyzz_add(acc, bgh::xyzz_from_words32<H>(plan.host_window_sums.data() + (size_t)w * PW));
+    const uint32_t* pw = plan.host_window_sums + (size_t)w * plan.J * 2 * PW;
+    bgh::Xyzz<H> s = bgh::xyzz_inf<H>(), run = bgh::xyzz_inf<H>(), jr = bgh::xyzz_inf<H>();
+    for (int j = (int)plan.J - 1; j >= 0; j--) {
+      s = bgh::xyzz_add(s, bgh::xyzz_from_words32<H>(pw + (size_t)(2 * j) * PW));
+      if (j >= 1) {
+        run = bgh::xyzz_add(run, bgh::xyzz_from_words32<H>(pw + (size_t)(2 * j + 1) * PW));
+        jr = bgh::xyzz_add(jr, run);  // sum_{j>=1} j R_j
+      }
+    }
+    for (uint32_t m = plan.part_span; m > 1; m >>= 1) jr = bgh::xyzz_dbl(jr);
+    acc = bgh::xyzz_add(acc, bgh::xyzz_add(s, jr));
   }
   bgh::aff_to_words32<H>(out_affine_words32, bgh::xyzz_to_affine(acc));
 }
 
+void msm_init_kernels() {
+  static bool done = false;
+  if (done) return;
+  BG_CUDA(cudaFuncSetAttribute(k_window_reduce<Fq>, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 32 * 4));
+  BG_CUDA(cudaFuncSetAttribute(k_window_reduce<Fq2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 64 * 4));
+  done = true;
+}
+
 template void msm_launch<Fq>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const uint32_t*, size_t,
-                             MsmPlan&);
+                             MsmPlan&, cudaStream_t);
 template void msm_launch<Fq2>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const uint32_t*, size_t,
-                              MsmPlan&);
+                              MsmPlan&, cudaStream_t);
 template void msm_fetch<Fq>(cudaStream_t, MsmPlan&);
 template void msm_fetch<Fq2>(cudaStream_t, MsmPlan&);
 template void msm_finish<Fq>(const MsmPlan&, uint32_t*);

@@ -11,19 +11,26 @@ struct MsmPlan {
   int c = 0;                              // window bits (0: pick from n)
   int W = 0;                              // windows
   size_t entries = 0;                     // bucket entries (n * W upper bound)
-  const uint32_t* d_window_sums = nullptr;  // W XYZZ points on the device
-  std::vector<uint32_t> host_window_sums;   // W XYZZ points after msm_fetch
+  uint32_t J = 1;                         // reduction parts per window
+  uint32_t part_span = 1;                 // buckets per part
+  const uint32_t* d_window_sums = nullptr;  // W x J x 2 XYZZ points on the device
+  cudaStream_t fetch_stream = nullptr;      // stream the reduction (and the copy) run on
+  // W XYZZ points after msm_fetch, in the context's pinned cache (a pageable destination
+  // would make the copy block the host and serialise the streams of a proof)
+  uint32_t* host_window_sums = nullptr;
 };
 
 int msm_pick_c(size_t n);
+void msm_init_kernels();
 void exclusive_scan(Workspace& ws, const std::string& tag, const uint32_t* d_in, uint32_t* d_out, size_t n,
                     cudaStream_t st, int depth);
 
-// Enqueue every device phase of one MSM on `st`; scratch buffers are named by `tag` so that
-// concurrent MSMs on different streams use different memory.
+// Enqueue every device phase of one MSM on `st` (the window reduction on `st_reduce` when
+// given, after an event); scratch buffers are named by `tag` so that MSMs in flight at the
+// same time use different memory.
 template <class F>
 void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
-                const uint32_t* d_scalars, size_t n, MsmPlan& plan);
+                const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce = nullptr);
 // Enqueue the copy of the window sums to the host.
 template <class F>
 void msm_fetch(cudaStream_t st, MsmPlan& plan);

@@ -343,48 +343,51 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   fr_from_mont(st, z, zc, nz);
   t_evals.stop(st);
 
-  // ---- fork the four MSMs that only need z
+  // ---- QAP on the main stream; it needs only the evaluation vectors
   BG_CUDA(cudaEventRecord(ctx.ev_fork, st));
-  MsmPlan plan[5];
-  struct Job {
-    int stream;
-    const char* tag;
-    bool g2;
-    const uint32_t* pts;
-    const uint32_t* sc;
-    size_t n;
-  };
-  const Job jobs[4] = {{0, "msm_a", false, pk.pa, zc, h.na},
-                       {1, "msm_b1", false, pk.pb1, zc, h.nb},
-                       {2, "msm_b2", true, pk.pb2, zc, h.nb},
-                       {3, "msm_l", false, pk.pl, zc + 8 * (size_t)h.ni, h.nl}};
-  const int plan_idx[4] = {0, 1, 2, 4};  // a, b1, b2, l; index 3 is msm_h
-  for (int j = 0; j < 4; j++) {
-    cudaStream_t s = ctx.side[jobs[j].stream];
-    BG_CUDA(cudaStreamWaitEvent(s, ctx.ev_fork, 0));
-    MsmPlan& p = plan[plan_idx[j]];
-    t_msm[plan_idx[j]].start(s);
-    if (jobs[j].g2) {
-      msm_launch<Fq2>(ctx, s, jobs[j].tag, jobs[j].pts, jobs[j].sc, jobs[j].n, p);
-      msm_fetch<Fq2>(s, p);
-    } else {
-      msm_launch<Fq>(ctx, s, jobs[j].tag, jobs[j].pts, jobs[j].sc, jobs[j].n, p);
-      msm_fetch<Fq>(s, p);
-    }
-    t_msm[plan_idx[j]].stop(s);
-  }
-
-  // ---- QAP on the main stream, then msm_h
   t_qap.start(st);
   uint32_t* hh = ws.get_t<uint32_t>("prove.h", d * 8);
   uint32_t* hc = ws.get_t<uint32_t>("prove.hc", d * 8);
   qap_h_run(ctx, st, ea, eb, ec, hh, h.lg);
   fr_from_mont(st, hh, hc, h.nh);
   t_qap.stop(st);
-  t_msm[3].start(st);
-  msm_launch<Fq>(ctx, st, "msm_h", pk.ph, hc, h.nh, plan[3]);
-  msm_fetch<Fq>(st, plan[3]);
-  t_msm[3].stop(st);
+  cudaEvent_t ev_qap = ctx.event("prove.qap_done");
+  BG_CUDA(cudaEventRecord(ev_qap, st));
+
+  // ---- MSM accumulations back to back on one stream (each one fills the GPU), every window
+  // reduction on a stream of its own so it overlaps the next accumulation; msm_h goes last
+  // because it waits for h
+  MsmPlan plan[5];  // a, b1, b2, h, l
+  struct Job {
+    int idx;
+    const char* tag;
+    bool g2;
+    const uint32_t* pts;
+    const uint32_t* sc;
+    size_t n;
+  };
+  const Job jobs[5] = {{0, "msm_a", false, pk.pa, zc, h.na},
+                       {1, "msm_b1", false, pk.pb1, zc, h.nb},
+                       {2, "msm_b2", true, pk.pb2, zc, h.nb},
+                       {4, "msm_l", false, pk.pl, zc + 8 * (size_t)h.ni, h.nl},
+                       {3, "msm_h", false, pk.ph, hc, h.nh}};
+  cudaStream_t acc_st = ctx.side[0];
+  BG_CUDA(cudaStreamWaitEvent(acc_st, ctx.ev_fork, 0));
+  for (int j = 0; j < 5; j++) {
+    const Job& jb = jobs[j];
+    cudaStream_t red = ctx.side[1 + j];
+    if (jb.idx == 3) BG_CUDA(cudaStreamWaitEvent(acc_st, ev_qap, 0));
+    MsmPlan& p = plan[jb.idx];
+    t_msm[jb.idx].start(acc_st);
+    if (jb.g2) {
+      msm_launch<Fq2>(ctx, acc_st, jb.tag, jb.pts, jb.sc, jb.n, p, red);
+      msm_fetch<Fq2>(acc_st, p);
+    } else {
+      msm_launch<Fq>(ctx, acc_st, jb.tag, jb.pts, jb.sc, jb.n, p, red);
+      msm_fetch<Fq>(acc_st, p);
+    }
+    t_msm[jb.idx].stop(red);
+  }
 
   // ---- host work that needs no MSM result, overlapped with the device
   uint64_t r[4], s[4], rs[4];
@@ -403,7 +406,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   const Xyzz<Fq2Ops> s_delta2 = bgh::xyzz_mul(dj2, s);
 
   // ---- join
-  for (int j = 0; j < 4; j++) BG_CUDA(cudaStreamSynchronize(ctx.side[jobs[j].stream]));
+  for (int j = 0; j < kStreams; j++) BG_CUDA(cudaStreamSynchronize(ctx.side[j]));
   BG_CUDA(cudaStreamSynchronize(st));
   check_status(ctx, st);
   uint32_t res[5][32];
