@@ -4,13 +4,14 @@
 // (Ev.matrix / matrix_a, groth16.bend:162-188, then Sc.canon, :214), qap (Pr.qap,
 // prove.bend:52-56), the five MSMs (prove.bend:64-117) and Groth.combine (groth16.bend:298-308).
 //
-// Device schedule (one context, one main stream + side streams):
-//   main:  witness H2D + repack -> evals (3 CSR SpMV) -> z canonical --fork--> qap_h -> h canonical -> msm_h
-//   side0: msm_a (pk_a, z)      side1: msm_b1 (pk_b1, z)     side2: msm_b2 (pk_b2, z, G2)
-//   side3: msm_l (pk_l, z[2..])
-// msm_a/b1/b2/l need only z and start while the QAP runs.  Each MSM ends with its window sums
-// on the host; the host runs the window Horner and the combine (a handful of scalar
-// multiplications; r*delta etc. are computed while the device works).
+// Device schedule (one context, the main stream + six side streams):
+//   main:   witness H2D + repack -> evals (3 CSR SpMV) -> z canonical -> qap_h -> h canonical
+//   side0:  MSM front ends and accumulations back to back (each fills the GPU):
+//           msm_a, msm_b1, msm_b2 (G2), msm_l (scalars z[ni..]), then msm_h once h is ready
+//   side1..5: each MSM's window reduction and result copy, overlapping the next accumulation
+// The QAP runs concurrently with the first accumulations.  The host finishes every MSM (window
+// Horner) as soon as its stream drains and assembles A, B and most of C (r delta, s delta,
+// s A + r B1, ...) while msm_h is still running, so only msm_h's finish is left at the end.
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -405,28 +406,32 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   const Xyzz<FqOps> rs_delta = bgh::xyzz_mul(dj, rs);
   const Xyzz<Fq2Ops> s_delta2 = bgh::xyzz_mul(dj2, s);
 
-  // ---- join
-  for (int j = 0; j < kStreams; j++) BG_CUDA(cudaStreamSynchronize(ctx.side[j]));
-  BG_CUDA(cudaStreamSynchronize(st));
-  check_status(ctx, st);
-  uint32_t res[5][32];
-  msm_finish<Fq>(plan[0], res[0]);
-  msm_finish<Fq>(plan[1], res[1]);
-  msm_finish<Fq2>(plan[2], res[2]);
-  msm_finish<Fq>(plan[3], res[3]);
-  msm_finish<Fq>(plan[4], res[4]);
-
-  // ---- combine (groth16.bend:298-308):
+  // ---- finish each MSM on the host as soon as its reduction stream drains (accumulation order
+  // a, b1, b2, l, h); everything that does not need msm_h -- A, B1, B2 and s A + r B1 - r s delta
+  // + mL -- is computed while msm_h is still on the device.  Combine (groth16.bend:298-308):
   // A = alpha + mA + r delta; B1 = beta + mB1 + s delta; B2 = beta2 + mB2 + s delta2;
   // C = s A + r B1 - r s delta + (mL + mH)
   auto g1 = [](const uint32_t* w) { return bgh::xyzz_from(bgh::aff_from_words32<FqOps>(w)); };
+  uint32_t res[5][32];
+  BG_CUDA(cudaStreamSynchronize(ctx.side[1]));
+  msm_finish<Fq>(plan[0], res[0]);
   const Xyzz<FqOps> A = bgh::xyzz_add(bgh::xyzz_add(g1(res[0]), r_delta), bgh::xyzz_from(pk.alpha));
+  BG_CUDA(cudaStreamSynchronize(ctx.side[2]));
+  msm_finish<Fq>(plan[1], res[1]);
   const Xyzz<FqOps> B1 = bgh::xyzz_add(bgh::xyzz_add(g1(res[1]), s_delta), bgh::xyzz_from(pk.beta));
+  Xyzz<FqOps> c_part = bgh::xyzz_add(bgh::xyzz_add(bgh::xyzz_mul(A, s), bgh::xyzz_mul(B1, r)), bgh::xyzz_neg(rs_delta));
+  BG_CUDA(cudaStreamSynchronize(ctx.side[3]));
+  msm_finish<Fq2>(plan[2], res[2]);
   const Xyzz<Fq2Ops> B2 = bgh::xyzz_add(
       bgh::xyzz_add(bgh::xyzz_from(bgh::aff_from_words32<Fq2Ops>(res[2])), s_delta2), bgh::xyzz_from(pk.beta2));
-  const Xyzz<FqOps> C = bgh::xyzz_add(
-      bgh::xyzz_add(bgh::xyzz_mul(A, s), bgh::xyzz_mul(B1, r)),
-      bgh::xyzz_add(bgh::xyzz_neg(rs_delta), bgh::xyzz_add(g1(res[4]), g1(res[3]))));
+  BG_CUDA(cudaStreamSynchronize(ctx.side[4]));
+  msm_finish<Fq>(plan[4], res[4]);
+  c_part = bgh::xyzz_add(c_part, g1(res[4]));
+  for (int j = 0; j < kStreams; j++) BG_CUDA(cudaStreamSynchronize(ctx.side[j]));
+  BG_CUDA(cudaStreamSynchronize(st));
+  check_status(ctx, st);
+  msm_finish<Fq>(plan[3], res[3]);
+  const Xyzz<FqOps> C = bgh::xyzz_add(c_part, g1(res[3]));
   wire_from_affine<FqOps>(out->a, bgh::xyzz_to_affine(A));
   wire_from_affine<Fq2Ops>(out->b, bgh::xyzz_to_affine(B2));
   wire_from_affine<FqOps>(out->c, bgh::xyzz_to_affine(C));
