@@ -34,7 +34,7 @@ EXPORTS = (
     "bg_pk_upload", "bg_pk_release", "bg_prove_resident", "bg_proof_format", "bg_ntt", "bg_field_op",
     "bg_curve_op", "bg_msm_g1_dev", "bg_msm_g2_dev", "bg_ntt_dev", "bg_repack_to_packed_dev",
     "bg_repack_to_wire_dev", "bg_synth_square_chain", "bg_msm_window_bits", "bg_ctx_profile",
-    "bg_ctx_kernel_stats", "bg_probe_imad",
+    "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc",
 )
 
 
@@ -104,6 +104,7 @@ def lib():
         "bg_ctx_profile": (i32, [vp, i32]),
         "bg_ctx_kernel_stats": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
         "bg_probe_imad": (i32, [vp, i32, u32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+        "bg_msm_g1_noalloc": (i32, [vp, vp, sz, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

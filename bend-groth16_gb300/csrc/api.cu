@@ -205,6 +205,13 @@ const char* bg_strerror(int status) {
 
 const char* bg_last_error(const bg_ctx* ctx) { return ctx ? ctx->c.last_error.c_str() : g_err_noctx.c_str(); }
 
+}  // extern "C"
+
+// message of the last failure of an entry point that takes no context (read with bg_last_error(NULL))
+void bg::set_noctx_error(const std::string& msg) { g_err_noctx = msg; }
+
+extern "C" {
+
 void* bg_ctx_stream(bg_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
 
 uint64_t bg_ctx_launches(const bg_ctx*) { return g_launches.load(); }

@@ -202,4 +202,6 @@ enum : uint32_t {
 
 inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
+void set_noctx_error(const std::string& msg);
+
 }  // namespace bg

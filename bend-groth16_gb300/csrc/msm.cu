@@ -23,6 +23,9 @@
 #include "host_ff.hpp"
 #include "msm.h"
 
+#include <cstring>
+#include <mutex>
+
 namespace bg {
 
 // ---------------------------------------------------------------- scan (exclusive, u32)
@@ -449,3 +452,150 @@ template void msm_finish<Fq>(const MsmPlan&, uint32_t*);
 template void msm_finish<Fq2>(const MsmPlan&, uint32_t*);
 
 }  // namespace bg
+
+// ---------------------------------------------------------------- allocation-free G1 MSM
+// bg_msm_g1_noalloc serves callers that must not allocate device memory at all: a host
+// program that has handed the whole GPU to its own memory pool and forbids any further
+// cudaMalloc, or a latency-critical loop in which the device-wide synchronisation that
+// cudaMalloc/cudaFree imply is not acceptable.  It runs the same kernels as the other MSM
+// entry points, but every scratch buffer is carved out of one fixed array that lives in the
+// library's own device image, so the call allocates nothing (no cudaMalloc, cudaFree,
+// pinned-host allocation or context).  The price is a hard size limit and shared state:
+//   * at most kNoAllocMaxPoints points (larger requests fail with BG_E_ARG);
+//   * every GPU that loads the library holds the kNoAllocScratchBytes array until the process
+//     exits;
+//   * all calls use the same array, which keeps the previous call's contents (the bucket
+//     counters are cleared at the start of each call); calls that overlap on the GPU race, so
+//     this entry point serialises calls made from one process and returns only when its work
+//     is complete;
+//   * the first call on a device looks up the array's device address on that device (the
+//     device current at the call); make that first call before any stream capture.
+namespace bg {
+namespace {
+
+constexpr size_t kNoAllocMaxPoints = size_t(1) << 14;
+constexpr size_t kNoAllocScratchBytes = size_t(9) << 20;  // the 2^14-point worst case needs 8.2 MiB
+constexpr size_t kNoAllocHostWords = 8192;                // window parts copied back for the Horner
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
+static uint32_t g_noalloc_host_parts[kNoAllocHostWords];
+static uint32_t g_noalloc_host_status;
+static void* g_noalloc_dev_ptr[kNoAllocMaxDevices];
+static std::mutex g_noalloc_mu;
+
+// device address of the scratch array on the current device (looked up once per device)
+uint8_t* noalloc_scratch() {
+  int dev = 0;
+  BG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) throw Error(BG_E_ARG, "bg_msm_g1_noalloc: device index out of range");
+  if (!g_noalloc_dev_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      throw Error(BG_E_DEVICE, std::string("bg_msm_g1_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+    g_noalloc_dev_ptr[dev] = p;
+  }
+  return static_cast<uint8_t*>(g_noalloc_dev_ptr[dev]);
+}
+
+void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t n, cudaStream_t st,
+                    uint32_t* out_aff32) {
+  constexpr int PW = 32;  // packed words of a G1 XYZZ point
+  if (n == 0) {
+    memset(out_aff32, 0, 16 * sizeof(uint32_t));
+    return;
+  }
+  if (n > kNoAllocMaxPoints)
+    throw Error(BG_E_ARG, "bg_msm_g1_noalloc: " + std::to_string(n) + " points exceed the fixed maximum of " +
+                              std::to_string(kNoAllocMaxPoints));
+  uint8_t* base = noalloc_scratch();
+  const int c = msm_pick_c(n);
+  const int W = 254 / c + 1;
+  const uint32_t nb = 1u << (c - 1);
+  const size_t nkeys = (size_t)W * nb;
+  const uint32_t K = kSlice<Fq>;
+  const size_t max_entries = n * (size_t)W;
+  const size_t max_threads = (max_entries + K - 1) / K;
+  const uint32_t RT = nb < 256 ? nb : 256;
+  const uint32_t M = (nb / RT) < 16 ? nb / RT : 16;
+  const uint32_t J = nb / (RT * M);
+  const unsigned tiles = ceil_div(nkeys + 1, kScanTile);
+
+  size_t off = 0;
+  auto carve = [&](size_t words) {
+    uint32_t* p = reinterpret_cast<uint32_t*>(base + off);
+    off += (words * sizeof(uint32_t) + 255) & ~size_t(255);
+    return p;
+  };
+  uint32_t* status = carve(1);
+  uint32_t* counts = carve(nkeys + 1);
+  uint32_t* offsets = carve(nkeys + 1);
+  uint32_t* cursor = carve(nkeys + 1);
+  uint32_t* tile_sums = carve(tiles);
+  uint32_t* tile_offs = carve(tiles);
+  uint32_t* sorted = carve(max_entries);
+  uint32_t* buckets = carve(nkeys * PW);
+  uint32_t* slot0 = carve(max_threads * PW);
+  uint32_t* slot1 = carve(max_threads * PW);
+  uint32_t* parts = carve((size_t)W * J * 2 * PW);
+  const size_t host_words = (size_t)W * J * 2 * PW;
+  if (off > kNoAllocScratchBytes || host_words > kNoAllocHostWords || tiles > (unsigned)kScanTile)
+    throw Error(BG_E_ARG, "bg_msm_g1_noalloc: scratch layout exceeds the fixed array");
+
+  // what must start at zero: the status word and the bucket counters
+  BG_CUDA(cudaMemsetAsync(status, 0, sizeof(uint32_t), st));
+  BG_CUDA(cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
+  k_digits_hist<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, counts, status);
+  BG_CHECK_LAUNCH();
+  if (tiles == 1) {
+    k_scan_tile<<<1, kScanThreads, 0, st>>>(counts, offsets, nullptr, nkeys + 1);
+    BG_CHECK_LAUNCH();
+  } else {
+    k_scan_tile<<<tiles, kScanThreads, 0, st>>>(counts, offsets, tile_sums, nkeys + 1);
+    BG_CHECK_LAUNCH();
+    k_scan_tile<<<1, kScanThreads, 0, st>>>(tile_sums, tile_offs, nullptr, tiles);
+    BG_CHECK_LAUNCH();
+    k_scan_add<<<ceil_div(nkeys + 1, 256), 256, 0, st>>>(offsets, tile_offs, nkeys + 1);
+    BG_CHECK_LAUNCH();
+  }
+  BG_CUDA(cudaMemcpyAsync(cursor, offsets, (nkeys + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+  k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, cursor, sorted);
+  BG_CHECK_LAUNCH();
+  k_bucket_acc<Fq><<<ceil_div(max_threads, 128), 128, 0, st>>>(d_points, offsets, sorted, (uint32_t)nkeys, K,
+                                                               buckets, slot0, slot1);
+  BG_CHECK_LAUNCH();
+  k_bucket_fixup<Fq><<<ceil_div(nkeys, 128), 128, 0, st>>>(offsets, (uint32_t)nkeys, K, slot0, slot1, buckets);
+  BG_CHECK_LAUNCH();
+  k_window_reduce<Fq><<<W * J, RT, RT * PW * sizeof(uint32_t), st>>>(buckets, nb, M, J, parts);
+  BG_CHECK_LAUNCH();
+  BG_CUDA(cudaMemcpyAsync(g_noalloc_host_parts, parts, host_words * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  BG_CUDA(cudaMemcpyAsync(&g_noalloc_host_status, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  BG_CUDA(cudaStreamSynchronize(st));
+  if (g_noalloc_host_status & BG_DSTATUS_SCALAR_RANGE)
+    throw Error(BG_E_ARG, "bg_msm_g1_noalloc: a scalar is not below 2^254 (not a canonical Fr)");
+  MsmPlan plan;
+  plan.c = c;
+  plan.W = W;
+  plan.J = J;
+  plan.part_span = RT * M;
+  plan.host_window_sums = g_noalloc_host_parts;
+  msm_finish<Fq>(plan, out_aff32);
+}
+
+}  // namespace
+}  // namespace bg
+
+extern "C" int bg_msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t n, void* stream,
+                                 uint32_t* out_aff32) {
+  if (!out_aff32 || (n && (!d_points || !d_scalars))) return BG_E_ARG;
+  std::lock_guard<std::mutex> lock(bg::g_noalloc_mu);
+  try {
+    bg::msm_g1_noalloc(d_points, d_scalars, n, static_cast<cudaStream_t>(stream), out_aff32);
+    return BG_OK;
+  } catch (const bg::Error& e) {
+    bg::set_noctx_error(e.what());
+    if (e.status == BG_E_DEVICE) cudaGetLastError();
+    return e.status;
+  }
+}

@@ -143,6 +143,19 @@ int bg_curve_op(bg_ctx* ctx, int curve, int op, const uint32_t* p16, const uint3
  * (8 words each), results affine packed (16 / 32 words) on the host. */
 int bg_msm_g1_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32);
 int bg_msm_g2_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32);
+/* G1 MSM that allocates nothing (no counterpart in the reference).  For callers that may not
+ * allocate device memory: a program whose GPU memory is all taken by its own pool, or a
+ * latency-critical loop that cannot afford the device synchronisation cudaMalloc and cudaFree
+ * imply.  Same inputs and result as bg_msm_g1_dev (device pointers to packed points and
+ * canonical scalars, affine result in 16 host words) but no context: scratch is a fixed
+ * 9 MiB array inside the library, held by every GPU that loads it until the process exits.
+ * n <= 16384 (larger n returns BG_E_ARG).  `stream` is a cudaStream_t or NULL.  All calls
+ * share the array (each clears what must start at zero); calls from one process are
+ * serialised and the function returns when its work is done, and calls that overlapped on the
+ * GPU would race.  The first call on a device looks up the array's address on the current
+ * device; make it before any stream capture.  Errors: bg_last_error(NULL). */
+int bg_msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t n, void* stream,
+                      uint32_t* out_aff32);
 int bg_ntt_dev(bg_ctx* ctx, uint32_t* d_data, uint32_t log2n, int mode);
 /* wire layout <-> packed layout for n elements (16 words -> 8 words), device pointers */
 int bg_repack_to_packed_dev(bg_ctx* ctx, const uint32_t* d_wire, uint32_t* d_packed, size_t n_elems);
