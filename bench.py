@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=18181818)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-primitives", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-proof mixed-K batch measurement")
     ap.add_argument("--msm-only", action="store_true",
                     help="time only the standalone G1 MSM 2^20 (a small, single-kernel-family profiling target)")
     ap.add_argument("--data-root", default=os.environ.get("BG_BENCH_DATA", "/tmp/bg_bench"))
@@ -274,6 +275,7 @@ def run_ours(args, dist: Dist):
 
     prims = None if args.no_primitives else primitives(ctx, files, nh, nb, args, ext, flush, imad_peak)
     roof_iso = prims.pop("roofline") if prims else None
+    batch = None if args.no_batch else batched(ctx, args, flush, ext)
 
     result = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -290,6 +292,7 @@ def run_ours(args, dist: Dist):
         "e2e": e2e, "roofline": roof_iso or roof, "roofline_in_proof": roof, "gpu_launches": int(launches), "clocks": clk,
         "phases_ms_median": {k: round(statistics.median(p[k] for p in phases), 3) for k in phases[0]},
         "kernels": kernel_ms, "fq_mul_rate_gops": round(fqmul_rate / 1e9, 2), "primitives": prims,
+        "batched": batch,
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(path, samples=1)
@@ -297,6 +300,99 @@ def run_ours(args, dist: Dist):
     files.free()
     ctx.close()
     return result
+
+
+BATCH_KS = (10, 12, 14, 16, 18)
+BATCH_WEIGHTS = (0.3, 0.25, 0.2, 0.15, 0.1)
+P_FR = 21888242871839275222246405745257275088548364400416034343698204186575808495617
+
+
+def shifted_witness(z_words, m: int):
+    """SquareChain witness for x0' = x_m, built from the instance witness
+    z = [1, x_N, x_0 .. x_{N-1}] (Montgomery wire words) and m more squarings of x_N:
+    z' = [1, x_{N+m}, x_m .. x_{N-1}, x_N .. x_{N+m-1}]"""
+    import numpy as np
+    import bendg
+    w = np.asarray(z_words, dtype=np.uint32).reshape(-1, 16)
+    r_inv = pow(1 << 256, -1, P_FR)
+    xn = bendg.wire_to_ints(w[1])[0] * r_inv % P_FR
+    ext = []
+    x = xn
+    for _ in range(m):
+        x = x * x % P_FR
+        ext.append(x)  # x_{N+1} .. x_{N+m}
+    mont = [v * (1 << 256) % P_FR for v in [xn] + ext]
+    tail = bendg.ints_to_wire(mont[:m])            # x_N .. x_{N+m-1}
+    head = bendg.ints_to_wire([mont[m]])           # x_{N+m}
+    return np.concatenate([w[0:1], head, w[2 + m:], tail]).reshape(-1)
+
+
+def batched(ctx, args, flush, ext):
+    """BASELINE configuration 3: 64 proofs of mixed K, one bg_prove_batch call versus the same
+    proofs made one at a time (plain), both against resident keys; every batched proof must
+    equal its plain twin bit for bit."""
+    import random
+
+    import numpy as np
+    import torch
+
+    import bendg
+    rng = random.Random(args.seed + 3)
+    keys, wits = {}, {}
+    files = {}
+    for k in BATCH_KS:
+        a = argparse.Namespace(**vars(args))
+        a.log2n = k
+        single = Dist.__new__(Dist)
+        single.world, single.rank, single.local, single.pg = 1, 0, 0, None
+        path = ensure_instance(a, single, lambda kk, s, p: ctx.synth_square_chain(kk, s, p))
+        files[k] = bendg.HostFiles(path)
+        keys[k] = ctx.pk_upload(files[k])
+        wits[k] = files[k].words("witness").copy()
+    ks = rng.choices(BATCH_KS, weights=BATCH_WEIGHTS, k=64)
+    jobs = []
+    for i, k in enumerate(ks):
+        w = shifted_witness(wits[k], 1 + i)
+        r, s = rng.randrange(P_FR), rng.randrange(P_FR)
+        rs = bendg.ints_to_wire([r * (1 << 256) % P_FR, s * (1 << 256) % P_FR]).reshape(-1)
+        jobs.append((k, w, rs))
+
+    def plain():
+        return [keys[k].prove(w, rs)[0] for k, w, rs in jobs]
+
+    def batch(lanes):
+        proofs, _, st = ctx.prove_batch([keys[k] for k, _, _ in jobs], [w for _, w, _ in jobs],
+                                        [rs for _, _, rs in jobs], lanes=lanes)
+        assert all(s == bendg.BG_OK for s in st)
+        return proofs
+
+    def timed(fn):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        out = fn()
+        e1.record(ext)
+        e1.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    plain(), batch(8)  # warm every lane and workspace
+    ref, t_plain = timed(plain)
+    lanes_best, t_best, got = None, None, None
+    for lanes in (4, 8, 12):
+        out, t = timed(lambda: batch(lanes))
+        if t_best is None or t < t_best:
+            lanes_best, t_best, got = lanes, t, out
+    exact = all(ctx.proof_text(a) == ctx.proof_text(b) for a, b in zip(got, ref))
+    for k in BATCH_KS:
+        keys[k].release()
+    return {"workload": "64 SquareChain proofs, K drawn from %s with weights %s (seed %d), resident keys"
+                        % (list(BATCH_KS), list(BATCH_WEIGHTS), args.seed + 3),
+            "k_counts": {str(k): ks.count(k) for k in BATCH_KS},
+            "plain_ms": round(t_plain, 2), "plain_proofs_per_s": round(64 / (t_plain * 1e-3), 1),
+            "batched_ms": round(t_best, 2), "batched_proofs_per_s": round(64 / (t_best * 1e-3), 1),
+            "speedup_vs_plain": round(t_plain / t_best, 3), "lanes": lanes_best,
+            "bit_exact_vs_plain": bool(exact)}
 
 
 def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):

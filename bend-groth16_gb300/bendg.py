@@ -34,7 +34,7 @@ EXPORTS = (
     "bg_pk_upload", "bg_pk_release", "bg_prove_resident", "bg_proof_format", "bg_ntt", "bg_field_op",
     "bg_curve_op", "bg_msm_g1_dev", "bg_msm_g2_dev", "bg_ntt_dev", "bg_repack_to_packed_dev",
     "bg_repack_to_wire_dev", "bg_synth_square_chain", "bg_msm_window_bits", "bg_ctx_profile",
-    "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc",
+    "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch",
 )
 
 
@@ -105,6 +105,8 @@ def lib():
         "bg_ctx_kernel_stats": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
         "bg_probe_imad": (i32, [vp, i32, u32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "bg_msm_g1_noalloc": (i32, [vp, vp, sz, vp, vp]),
+        "bg_prove_batch": (i32, [vp, vp, vp, vp, sz, i32, ctypes.POINTER(Proof), ctypes.POINTER(PhaseMs),
+                                 ctypes.POINTER(i32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -257,6 +259,32 @@ class Context:
         h = ctypes.c_void_p()
         self._check(self._L.bg_pk_upload(self.h, ctypes.byref(files.inputs), ctypes.byref(h)), "bg_pk_upload")
         return ResidentKey(self, h)
+
+    def prove_batch(self, keys, witnesses, rss, lanes: int = 8):
+        """proofs i = (keys[i], witnesses[i], rss[i]) made concurrently; witnesses / rss are
+        numpy uint32 arrays (host) or integer pointers (host or device).
+        Returns (proofs, phase dicts, statuses)."""
+        n = len(keys)
+        keep = []  # host arrays stay referenced until the call returns
+
+        def ptr(x):
+            if isinstance(x, int):
+                return x
+            a = _u32(x)
+            keep.append(a)
+            return a.ctypes.data
+
+        PK = ctypes.c_void_p * n
+        PP = ctypes.c_void_p * n
+        pks = PK(*[k.h.value for k in keys])
+        ws = PP(*[ptr(w) for w in witnesses])
+        rs = PP(*[ptr(r) for r in rss])
+        proofs = (Proof * n)()
+        times = (PhaseMs * n)()
+        st = (ctypes.c_int * n)()
+        self._check(self._L.bg_prove_batch(self.h, pks, ws, rs, n, lanes, proofs, times, st), "bg_prove_batch")
+        del keep
+        return list(proofs), [t.as_dict() for t in times], list(st)
 
     def synth_square_chain(self, log2n: int, seed: int, path: str):
         os.makedirs(path, exist_ok=True)

@@ -1,9 +1,13 @@
 // extern "C" entry points of include/bg.h: argument checks, host <-> device staging in the
 // wire layout of bend2/FORMAT.md, and the mapping of exceptions to BG_E_* statuses.
+#include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -21,6 +25,8 @@ void synth_square_chain(Ctx& c, uint32_t log2n, uint64_t seed, const std::string
 
 struct bg_ctx {
   bg::Ctx c;
+  // lanes of bg_prove_batch: each a context of its own (streams, workspace), created on demand
+  std::vector<std::unique_ptr<bg::Ctx>> lanes;
 };
 struct bg_pk {
   bg::PkDev* pk;
@@ -128,6 +134,46 @@ void msm_dev(Ctx& c, const uint32_t* d_points, const uint32_t* d_scalars, size_t
   msm_finish<F>(plan, out_aff32);
 }
 
+// streams, events and the status word of one context on `device`
+void ctx_init(Ctx& c, int device) {
+  int ndev = 0;
+  BG_CUDA(cudaGetDeviceCount(&ndev));
+  require(device >= 0 && device < ndev, "bg_ctx_create: no such CUDA device");
+  BG_CUDA(cudaSetDevice(device));
+  c.device = device;
+  BG_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
+  BG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  for (int i = 0; i < kStreams; i++) {
+    BG_CUDA(cudaStreamCreateWithFlags(&c.side[i], cudaStreamNonBlocking));
+    BG_CUDA(cudaEventCreateWithFlags(&c.ev_join[i], cudaEventDisableTiming));
+  }
+  BG_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
+  c.d_status = c.ws.get_t<uint32_t>("status", 1);
+  BG_CUDA(cudaMemsetAsync(c.d_status, 0, 4, c.stream));
+  BG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void ctx_release(Ctx& c) {
+  cudaSetDevice(c.device);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  for (int i = 0; i < kStreams; i++) {
+    if (c.side[i]) {
+      cudaStreamSynchronize(c.side[i]);
+      cudaStreamDestroy(c.side[i]);
+      c.side[i] = nullptr;
+    }
+    if (c.ev_join[i]) cudaEventDestroy(c.ev_join[i]);
+    c.ev_join[i] = nullptr;
+  }
+  if (c.ev_fork) cudaEventDestroy(c.ev_fork);
+  c.ev_fork = nullptr;
+  for (auto& kv : c.events) cudaEventDestroy(kv.second);
+  c.events.clear();
+  c.ws.clear();
+  if (c.stream) cudaStreamDestroy(c.stream);
+  c.stream = nullptr;
+}
+
 bool read_file(const std::string& path, std::vector<char>& out) {
   FILE* f = fopen(path.c_str(), "rb");
   if (!f) return false;
@@ -148,23 +194,7 @@ int bg_ctx_create(int device, bg_ctx** out) {
   if (!out) return BG_E_ARG;
   *out = nullptr;
   bg_ctx* ctx = new bg_ctx();
-  int st = guard(nullptr, [&] {
-    int ndev = 0;
-    BG_CUDA(cudaGetDeviceCount(&ndev));
-    require(device >= 0 && device < ndev, "bg_ctx_create: no such CUDA device");
-    BG_CUDA(cudaSetDevice(device));
-    ctx->c.device = device;
-    BG_CUDA(cudaDeviceGetAttribute(&ctx->c.sm_count, cudaDevAttrMultiProcessorCount, device));
-    BG_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
-    for (int i = 0; i < kStreams; i++) {
-      BG_CUDA(cudaStreamCreateWithFlags(&ctx->c.side[i], cudaStreamNonBlocking));
-      BG_CUDA(cudaEventCreateWithFlags(&ctx->c.ev_join[i], cudaEventDisableTiming));
-    }
-    BG_CUDA(cudaEventCreateWithFlags(&ctx->c.ev_fork, cudaEventDisableTiming));
-    ctx->c.d_status = ctx->c.ws.get_t<uint32_t>("status", 1);
-    BG_CUDA(cudaMemsetAsync(ctx->c.d_status, 0, 4, ctx->c.stream));
-    BG_CUDA(cudaStreamSynchronize(ctx->c.stream));
-  });
+  int st = guard(nullptr, [&] { ctx_init(ctx->c, device); });
   if (st != BG_OK) {
     delete ctx;
     return st;
@@ -175,18 +205,9 @@ int bg_ctx_create(int device, bg_ctx** out) {
 
 void bg_ctx_destroy(bg_ctx* ctx) {
   if (!ctx) return;
-  cudaSetDevice(ctx->c.device);
-  cudaStreamSynchronize(ctx->c.stream);
-  for (int i = 0; i < kStreams; i++) {
-    if (ctx->c.side[i]) {
-      cudaStreamSynchronize(ctx->c.side[i]);
-      cudaStreamDestroy(ctx->c.side[i]);
-    }
-    if (ctx->c.ev_join[i]) cudaEventDestroy(ctx->c.ev_join[i]);
-  }
-  if (ctx->c.ev_fork) cudaEventDestroy(ctx->c.ev_fork);
-  ctx->c.ws.clear();
-  if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
+  for (auto& lane : ctx->lanes) ctx_release(*lane);
+  ctx->lanes.clear();
+  ctx_release(ctx->c);
   delete ctx;
 }
 
@@ -384,6 +405,48 @@ int bg_prove_resident(bg_ctx* ctx, bg_pk* pk, const uint32_t* witness16, const u
   });
 }
 
+int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnesses, const uint32_t* const* rs,
+                   size_t count, int lanes, bg_proof* out, bg_phase_ms* times, int* statuses) {
+  if (!ctx || (count && (!pks || !witnesses || !rs || !out || !statuses)) || lanes < 1 || lanes > 32)
+    return BG_E_ARG;
+  for (size_t i = 0; i < count; i++)
+    if (!pks[i] || !witnesses[i] || !rs[i] || pks[i]->owner != ctx) return BG_E_ARG;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    while ((int)ctx->lanes.size() < lanes) {
+      std::unique_ptr<Ctx> lane(new Ctx());
+      ctx_init(*lane, ctx->c.device);
+      ctx->lanes.push_back(std::move(lane));
+    }
+    // largest domains first (longest-processing-time order) so the tail is made of small proofs
+    std::vector<size_t> order(count);
+    for (size_t i = 0; i < count; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return pks[a]->pk->h.lg > pks[b]->pk->h.lg; });
+    std::atomic<size_t> next{0};
+    auto work = [&](Ctx* lane) {
+      cudaSetDevice(lane->device);
+      for (;;) {
+        const size_t k = next.fetch_add(1);
+        if (k >= count) return;
+        const size_t i = order[k];
+        try {
+          prove_resident(*lane, *pks[i]->pk, witnesses[i], rs[i], &out[i], times ? &times[i] : nullptr, 0.0);
+          statuses[i] = BG_OK;
+        } catch (const Error& e) {
+          statuses[i] = e.status;
+          if (e.status == BG_E_DEVICE) cudaGetLastError();
+        } catch (...) {
+          statuses[i] = BG_E_DEVICE;
+        }
+      }
+    };
+    std::vector<std::thread> threads;
+    for (int l = 0; l < lanes; l++) threads.emplace_back(work, ctx->lanes[l].get());
+    for (auto& t : threads) t.join();
+  });
+}
+
 int bg_prove_host(bg_ctx* ctx, const bg_inputs* in, bg_proof* out, bg_phase_ms* times) {
   if (!ctx || !in || !out) return BG_E_ARG;
   return guard(ctx, [&] {
@@ -489,7 +552,7 @@ int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, doubl
 }
 
 int bg_probe_imad(bg_ctx* ctx, int which, uint32_t iters, double* ops, double* ms) {
-  if (!ctx || !ops || !ms || (which != 0 && which != 1) || iters == 0) return BG_E_ARG;
+  if (!ctx || !ops || !ms || which < 0 || which > 4 || iters == 0) return BG_E_ARG;
   return guard(ctx, [&] {
     Ctx& c = ctx->c;
     cudaSetDevice(c.device);
@@ -507,7 +570,7 @@ int bg_probe_imad(bg_ctx* ctx, int which, uint32_t iters, double* ops, double* m
     BG_CUDA(cudaEventElapsedTime(&t, a, b));
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    const double per_thread = which == 0 ? 16.0 * iters : 4.0 * iters;
+    const double per_thread = which == 1 ? 4.0 * iters : 16.0 * iters;
     *ops = per_thread * threads * blocks;
     *ms = t;
   });

@@ -228,11 +228,44 @@ __global__ void k_fqmul_probe(uint32_t* __restrict__ sink, uint32_t iters, uint3
   if (o == 0x12345678u) sink[0] = o;
 }
 
+// single-form chains: 16 independent accumulators, one instruction form each
+// (form 2: mad.lo.u32, 3: mad.hi.u32, 4: mad.wide.u32 into 64-bit accumulators)
+template <int FORM>
+__global__ void k_imad_form_probe(uint32_t* __restrict__ sink, uint32_t iters, uint32_t seed) {
+  uint32_t a[16];
+  unsigned long long w[16];
+  const uint32_t b = seed * 2654435761u + threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    a[j] = seed ^ (threadIdx.x * 7919u + j);
+    w[j] = a[j];
+  }
+  for (uint32_t it = 0; it < iters; it++) {
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      if (FORM == 2) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[j]) : "r"(b), "r"(a[(j + 5) & 15]));
+      if (FORM == 3) asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(a[j]) : "r"(b), "r"(a[(j + 5) & 15]));
+      if (FORM == 4) asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(w[j]) : "r"(a[j]), "r"(b));
+    }
+    if (FORM == 4) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) a[j] ^= (uint32_t)(w[j] >> 32);
+    }
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int j = 0; j < 16; j++) x ^= a[j] ^ (uint32_t)w[j];
+  if (x == 0x12345678u) sink[0] = x;
+}
+
 void imad_probe(cudaStream_t st, int blocks, int threads, uint32_t iters, uint32_t* sink, int which) {
-  if (which == 0)
-    k_imad_probe<<<blocks, threads, 0, st>>>(sink, iters, 12345u);
-  else
-    k_fqmul_probe<<<blocks, threads, 0, st>>>(sink, iters, 12345u);
+  switch (which) {
+    case 0: k_imad_probe<<<blocks, threads, 0, st>>>(sink, iters, 12345u); break;
+    case 1: k_fqmul_probe<<<blocks, threads, 0, st>>>(sink, iters, 12345u); break;
+    case 2: k_imad_form_probe<2><<<blocks, threads, 0, st>>>(sink, iters, 12345u); break;
+    case 3: k_imad_form_probe<3><<<blocks, threads, 0, st>>>(sink, iters, 12345u); break;
+    default: k_imad_form_probe<4><<<blocks, threads, 0, st>>>(sink, iters, 12345u); break;
+  }
   BG_CHECK_LAUNCH();
 }
 

@@ -124,6 +124,13 @@ void bg_pk_release(bg_pk* pk);
 /* A proof against a resident key; witness16 / rs16 are host buffers (witness.bin, rs.bin). */
 int bg_prove_resident(bg_ctx* ctx, bg_pk* pk, const uint32_t* witness16, const uint32_t* rs16, bg_proof* out,
                       bg_phase_ms* times);
+/* Many proofs at once against resident keys (no counterpart in the reference, which proves one
+ * proof per process): `lanes` concurrent provers (1..32, each with its own streams and
+ * workspace) take the proofs largest domain first; small proofs share the GPU instead of
+ * leaving it idle.  out[i], times[i] (times may be NULL) and statuses[i] belong to proof i;
+ * every result is bit-identical to the same proof made alone. */
+int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnesses16, const uint32_t* const* rs16,
+                   size_t count, int lanes, bg_proof* out, bg_phase_ms* times, int* statuses);
 /* Proof line text exactly as the reference prints it: "A x y\nB x0 x1 y0 y1\nC x y\n"
  * (canonical big-endian 0x + 64 hex digits, bend2/FORMAT.md:33).  buf needs >= 600 bytes. */
 int bg_proof_format(const bg_proof* proof, char* buf, size_t buf_bytes);
@@ -177,9 +184,9 @@ int bg_ctx_profile(bg_ctx* ctx, int enable);
  * "msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_reduce_g1", "msm_reduce_g2", "msm_digits",
  * "msm_scatter", "ntt_pass".  Unknown names report zero launches. */
 int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms);
-/* Integer multiply-add throughput probe: which = 0 raw 32-bit mad.lo/mad.hi chains,
- * which = 1 Fq Montgomery products.  Returns the operations executed (32-bit IMADs, or Fq
- * products) and the kernel time in ms. */
+/* Integer multiply-add throughput probe: which = 0 raw 32-bit mad.lo/mad.hi chains (50/50),
+ * 1 Fq Montgomery products, 2 mad.lo only, 3 mad.hi only, 4 mad.wide.u32 only.  Returns the
+ * operations executed (instructions, or Fq products for 1) and the kernel time in ms. */
 int bg_probe_imad(bg_ctx* ctx, int which, uint32_t iters, double* ops, double* ms);
 
 #ifdef __cplusplus

@@ -1,0 +1,32 @@
+"""Host logic of bench.py (no GPU): the shifted SquareChain witnesses used for the 64-proof
+batch satisfy the circuit, and the instance generator's witness layout is what they assume."""
+import ctypes
+import os
+
+import numpy as np
+
+import bench
+import bn254_ref as o
+import oracle_c
+import oracle_io
+
+
+def test_shifted_witness_satisfies_square_chain(tmp_path):
+    L = oracle_c.lib()
+    L.bgo_synth_square_chain.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_int]
+    assert L.bgo_synth_square_chain(5, 11, str(tmp_path).encode(), 2) == 0
+    z_words = np.fromfile(os.path.join(tmp_path, "witness.bin"), dtype="<u4").astype(np.uint32)
+    n = 1 << 5
+    for m in (1, 2, 7):
+        w = bench.shifted_witness(z_words, m)
+        z = oracle_io.fes(w.astype("<u4").tobytes(), n + 2, o.P_FR)
+        assert z[0] == 1
+        xs = z[2:]
+        assert all(xs[i + 1] == xs[i] * xs[i] % o.P_FR for i in range(n - 1))
+        assert z[1] == xs[-1] * xs[-1] % o.P_FR  # x_N' = x_{N-1}'^2 (the last constraint)
+        z0 = oracle_io.fes(z_words.astype("<u4").tobytes(), n + 2, o.P_FR)
+        assert xs[0] == pow(z0[2], 2 ** m, o.P_FR)  # x_0' = x_m of the original chain
+
+
+def test_batch_weights():
+    assert abs(sum(bench.BATCH_WEIGHTS) - 1.0) < 1e-12 and len(bench.BATCH_KS) == 5
