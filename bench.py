@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-primitives", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-proof mixed-K batch measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the Poisson-arrival serving measurement")
     ap.add_argument("--msm-only", action="store_true",
                     help="time only the standalone G1 MSM 2^20 (a small, single-kernel-family profiling target)")
     ap.add_argument("--data-root", default=os.environ.get("BG_BENCH_DATA", "/tmp/bg_bench"))
@@ -276,6 +277,7 @@ def run_ours(args, dist: Dist):
     prims = None if args.no_primitives else primitives(ctx, files, nh, nb, args, ext, flush, imad_peak)
     roof_iso = prims.pop("roofline") if prims else None
     batch = None if args.no_batch else batched(ctx, args, flush, ext)
+    serve = None if args.no_serve else serving(ctx, args)
 
     result = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -292,7 +294,7 @@ def run_ours(args, dist: Dist):
         "e2e": e2e, "roofline": roof_iso or roof, "roofline_in_proof": roof, "gpu_launches": int(launches), "clocks": clk,
         "phases_ms_median": {k: round(statistics.median(p[k] for p in phases), 3) for k in phases[0]},
         "kernels": kernel_ms, "fq_mul_rate_gops": round(fqmul_rate / 1e9, 2), "primitives": prims,
-        "batched": batch,
+        "batched": batch, "serving": serve,
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(path, samples=1)
@@ -393,6 +395,97 @@ def batched(ctx, args, flush, ext):
             "batched_ms": round(t_best, 2), "batched_proofs_per_s": round(64 / (t_best * 1e-3), 1),
             "speedup_vs_plain": round(t_plain / t_best, 3), "lanes": lanes_best,
             "bit_exact_vs_plain": bool(exact)}
+
+
+SERVE_KS = (12, 14, 16, 18, 20)
+SERVE_WEIGHTS = (0.3, 0.25, 0.2, 0.15, 0.1)
+SERVE_RATES = (10, 50, 100, 200, 500)
+
+
+def percentile(xs, q):
+    s = sorted(xs)
+    if not s:
+        return None
+    i = min(len(s) - 1, max(0, int(round(q / 100.0 * (len(s) - 1)))))
+    return s[i]
+
+
+def serving(ctx, args, lanes=8, seconds=1.5):
+    """BASELINE configuration 4: Poisson arrivals of prove requests with K drawn from
+    SERVE_KS, all five proving keys resident, continuous batching in the library's server;
+    p50 / p99 latency (submit -> proof) and completed proofs/s per offered rate."""
+    import random
+    import threading
+
+    import bendg
+    rng = random.Random(args.seed + 4)
+    keys, pools = {}, {}
+    for k in SERVE_KS:
+        a = argparse.Namespace(**vars(args))
+        a.log2n = k
+        single = Dist.__new__(Dist)
+        single.world, single.rank, single.local, single.pg = 1, 0, 0, None
+        path = ensure_instance(a, single, lambda kk, s, p: ctx.synth_square_chain(kk, s, p))
+        f = bendg.HostFiles(path)
+        keys[k] = ctx.pk_upload(f)
+        z = f.words("witness").copy()
+        pools[k] = [shifted_witness(z, 1 + j) for j in range(4)]  # distinct valid witnesses
+        del f
+    budget = 64 << 30
+    srv = bendg.Server(ctx, lanes=lanes, hbm_budget_bytes=budget)
+    # warm every lane on the largest key
+    for t in range(lanes):
+        srv.submit(keys[SERVE_KS[-1]], pools[SERVE_KS[-1]][0], bendg.ints_to_wire([1, 1]).reshape(-1), 10**9 + t)
+    for _ in range(lanes):
+        srv.wait(600000)
+    results = []
+    tag = 0
+    for rate in SERVE_RATES:
+        n = max(12, int(rate * seconds))
+        arrivals, t = [], 0.0
+        for _ in range(n):
+            t += rng.expovariate(rate)
+            arrivals.append(t)
+        reqs = []
+        for _ in range(n):
+            k = rng.choices(SERVE_KS, weights=SERVE_WEIGHTS, k=1)[0]
+            rs = bendg.ints_to_wire([rng.randrange(P_FR) * (1 << 256) % P_FR,
+                                     rng.randrange(P_FR) * (1 << 256) % P_FR]).reshape(-1)
+            reqs.append((tag, k, rng.choice(pools[k]), rs))
+            tag += 1
+        lat, done_at = {}, []
+
+        def collect():
+            while len(lat) < n:
+                r = srv.wait(600000)
+                if r is None:
+                    return
+                assert r[5] == bendg.BG_OK
+                lat[r[0]] = r[3]
+                done_at.append(time.perf_counter())
+
+        th = threading.Thread(target=collect)
+        th.start()
+        t0 = time.perf_counter()
+        for (tg, k, w, rs), at in zip(reqs, arrivals):
+            now = time.perf_counter() - t0
+            if at > now:
+                time.sleep(at - now)
+            srv.submit(keys[k], w, rs, tg)
+        th.join()
+        span = max(done_at) - t0
+        vals = list(lat.values())
+        results.append({"offered_rps": rate, "requests": n, "completed": len(vals),
+                        "p50_ms": round(percentile(vals, 50), 2), "p99_ms": round(percentile(vals, 99), 2),
+                        "mean_ms": round(sum(vals) / len(vals), 2), "proofs_per_s": round(len(vals) / span, 1),
+                        "k_counts": {str(k): sum(1 for r in reqs if r[1] == k) for k in SERVE_KS}})
+    reserved = srv.reserved_bytes()
+    srv.close()
+    for k in SERVE_KS:
+        keys[k].release()
+    return {"workload": "Poisson arrivals, K drawn from %s with weights %s (seed %d), %s s of arrivals per rate, "
+                        "all five keys resident" % (list(SERVE_KS), list(SERVE_WEIGHTS), args.seed + 4, seconds),
+            "lanes": lanes, "hbm_budget_bytes": budget, "reserved_scratch_bytes": reserved, "rates": results}
 
 
 def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):

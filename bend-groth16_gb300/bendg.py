@@ -34,7 +34,8 @@ EXPORTS = (
     "bg_pk_upload", "bg_pk_release", "bg_prove_resident", "bg_proof_format", "bg_ntt", "bg_field_op",
     "bg_curve_op", "bg_msm_g1_dev", "bg_msm_g2_dev", "bg_ntt_dev", "bg_repack_to_packed_dev",
     "bg_repack_to_wire_dev", "bg_synth_square_chain", "bg_msm_window_bits", "bg_ctx_profile",
-    "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch",
+    "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch", "bg_prove_footprint",
+    "bg_server_create", "bg_server_submit", "bg_server_wait", "bg_server_reserved_bytes", "bg_server_destroy",
 )
 
 
@@ -107,6 +108,14 @@ def lib():
         "bg_msm_g1_noalloc": (i32, [vp, vp, sz, vp, vp]),
         "bg_prove_batch": (i32, [vp, vp, vp, vp, sz, i32, ctypes.POINTER(Proof), ctypes.POINTER(PhaseMs),
                                  ctypes.POINTER(i32)]),
+        "bg_prove_footprint": (sz, [vp]),
+        "bg_server_create": (i32, [vp, i32, sz, ctypes.POINTER(vp)]),
+        "bg_server_submit": (i32, [vp, vp, vp, vp, u64]),
+        "bg_server_wait": (i32, [vp, i32, ctypes.POINTER(u64), ctypes.POINTER(Proof), ctypes.POINTER(PhaseMs),
+                                 ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(i32)]),
+        "bg_server_reserved_bytes": (sz, [vp]),
+        "bg_server_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -313,9 +322,55 @@ class Context:
         self._check(self._L.bg_repack_to_packed_dev(self.h, d_wire, d_packed, n), "bg_repack_to_packed_dev")
 
 
+class Server:
+    """Continuous-batching prove server over resident keys (bg_server_*)."""
+
+    def __init__(self, ctx: Context, lanes: int = 8, hbm_budget_bytes: int = 64 << 30):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        ctx._check(ctx._L.bg_server_create(ctx.h, lanes, hbm_budget_bytes, ctypes.byref(h)), "bg_server_create")
+        self.h = h
+        self._keep = {}
+
+    def submit(self, key: "ResidentKey", witness16, rs16, tag: int):
+        w, r = _u32(witness16), _u32(rs16)
+        self._keep[tag] = (w, r)  # the buffers must outlive the request
+        self.ctx._check(self.ctx._L.bg_server_submit(self.h, key.h, _ptr(w), _ptr(r), tag), "bg_server_submit")
+
+    def wait(self, timeout_ms: int = 60000):
+        """-> (tag, proof, phases, latency_ms, queue_ms, status) or None on timeout"""
+        tag = ctypes.c_uint64()
+        proof, t = Proof(), PhaseMs()
+        lat, q, st = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        rc = self.ctx._L.bg_server_wait(self.h, timeout_ms, ctypes.byref(tag), ctypes.byref(proof), ctypes.byref(t),
+                                        ctypes.byref(lat), ctypes.byref(q), ctypes.byref(st))
+        if rc == BG_E_TIMEOUT:
+            return None
+        self.ctx._check(rc, "bg_server_wait")
+        self._keep.pop(tag.value, None)
+        return tag.value, proof, t.as_dict(), lat.value, q.value, st.value
+
+    def reserved_bytes(self) -> int:
+        return int(self.ctx._L.bg_server_reserved_bytes(self.h))
+
+    def close(self):
+        if self.h:
+            self.ctx._L.bg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class ResidentKey:
     def __init__(self, ctx: Context, h):
         self.ctx, self.h = ctx, h
+
+    def footprint(self) -> int:
+        return int(self.ctx._L.bg_prove_footprint(self.h))
 
     def prove(self, witness16: np.ndarray, rs16: np.ndarray):
         proof, t = Proof(), PhaseMs()

@@ -32,6 +32,10 @@ struct bg_pk {
   bg::PkDev* pk;
   bg_ctx* owner;
 };
+struct bg_server {
+  bg::Server* s;
+  bg_ctx* owner;
+};
 
 using namespace bg;
 
@@ -134,6 +138,10 @@ void msm_dev(Ctx& c, const uint32_t* d_points, const uint32_t* d_scalars, size_t
   msm_finish<F>(plan, out_aff32);
 }
 
+}  // namespace
+
+namespace bg {
+
 // streams, events and the status word of one context on `device`
 void ctx_init(Ctx& c, int device) {
   int ndev = 0;
@@ -173,6 +181,10 @@ void ctx_release(Ctx& c) {
   if (c.stream) cudaStreamDestroy(c.stream);
   c.stream = nullptr;
 }
+
+}  // namespace bg
+
+namespace {
 
 bool read_file(const std::string& path, std::vector<char>& out) {
   FILE* f = fopen(path.c_str(), "rb");
@@ -445,6 +457,36 @@ int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnes
     for (int l = 0; l < lanes; l++) threads.emplace_back(work, ctx->lanes[l].get());
     for (auto& t : threads) t.join();
   });
+}
+
+size_t bg_prove_footprint(const bg_pk* pk) { return pk ? prove_footprint(pk->pk->h) : 0; }
+
+int bg_server_create(bg_ctx* ctx, int lanes, size_t hbm_budget_bytes, bg_server** out) {
+  if (!ctx || !out || lanes < 1 || lanes > 32 || hbm_budget_bytes == 0) return BG_E_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    cudaSetDevice(ctx->c.device);
+    *out = new bg_server{server_create(ctx->c.device, lanes, hbm_budget_bytes), ctx};
+  });
+}
+
+int bg_server_submit(bg_server* s, bg_pk* pk, const uint32_t* witness16, const uint32_t* rs16, uint64_t tag) {
+  if (!s || !pk || !witness16 || !rs16 || pk->owner != s->owner) return BG_E_ARG;
+  return guard(s->owner, [&] { server_submit(s->s, pk->pk, witness16, rs16, tag); });
+}
+
+int bg_server_wait(bg_server* s, int timeout_ms, uint64_t* tag, bg_proof* out, bg_phase_ms* times,
+                   double* latency_ms, double* queue_ms, int* status) {
+  if (!s || !tag || !status || timeout_ms < 0) return BG_E_ARG;
+  return server_wait(s->s, timeout_ms, tag, out, times, latency_ms, queue_ms, status) ? BG_OK : BG_E_TIMEOUT;
+}
+
+size_t bg_server_reserved_bytes(bg_server* s) { return s ? server_reserved(s->s) : 0; }
+
+void bg_server_destroy(bg_server* s) {
+  if (!s) return;
+  server_destroy(s->s);
+  delete s;
 }
 
 int bg_prove_host(bg_ctx* ctx, const bg_inputs* in, bg_proof* out, bg_phase_ms* times) {

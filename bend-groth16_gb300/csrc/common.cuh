@@ -203,5 +203,8 @@ enum : uint32_t {
 inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
 void set_noctx_error(const std::string& msg);
+// create / destroy the streams, events and workspace of a context on `device`
+void ctx_init(Ctx& c, int device);
+void ctx_release(Ctx& c);
 
 }  // namespace bg

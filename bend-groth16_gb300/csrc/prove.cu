@@ -451,6 +451,31 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   }
 }
 
+// ---------------------------------------------------------------- scratch footprint
+// Device bytes one proof's workspace needs (the buffers msm_launch, qap_h_run and
+// prove_resident request), used for admission control; a 10% margin covers rounding.
+static size_t msm_footprint(size_t n, bool g2) {
+  if (n == 0) return 0;
+  const int c = msm_pick_c(n);
+  const size_t W = 254 / c + 1, nb = size_t(1) << (c - 1), nkeys = W * nb;
+  const size_t PW = g2 ? 64 : 32, K = g2 ? 16 : 32;
+  const size_t entries = n * W, threads = (entries + K - 1) / K;
+  const size_t RT = nb < 256 ? nb : 256, M = (nb / RT) < 16 ? nb / RT : 16, J = nb / (RT * M);
+  const size_t words = 3 * (nkeys + 1) + entries + nkeys * PW + 2 * threads * PW + W * J * 2 * PW +
+                       2 * ((nkeys + 1) / 2048 + 1);
+  return words * 4;
+}
+
+size_t prove_footprint(const Header& h) {
+  const size_t d = size_t(1) << h.lg, nz = (size_t)h.ni + h.nw;
+  size_t b = nz * (64 + 32 + 32)          // witness wire, packed, canonical
+             + 5 * d * 32                 // ea, eb, ec, h, h canonical
+             + d * 32 + 4096 * 32;        // twiddle tables (w^i and w^-i, n/2 each) + coset tables
+  b += msm_footprint(h.na, false) + msm_footprint(h.nb, false) + msm_footprint(h.nb, true) +
+       msm_footprint(h.nh, false) + msm_footprint(h.nl, false);
+  return b + b / 10 + (4u << 20);
+}
+
 // ---------------------------------------------------------------- proof text
 int format_proof(const bg_proof* p, char* buf, size_t cap) {
   auto hex = [](const uint32_t* w16, bool mont_fq, char* o) {

@@ -34,5 +34,16 @@ void check_status(Ctx& ctx, cudaStream_t st);
 void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32_t* rs16, bg_proof* out,
                     bg_phase_ms* times, double load_ms_before);
 int format_proof(const bg_proof* p, char* buf, size_t cap);
+// device bytes of scratch one proof against a key with this header needs
+size_t prove_footprint(const Header& h);
+
+// serving loop (server.cu)
+class Server;
+Server* server_create(int device, int lanes, size_t budget);
+void server_destroy(Server* s);
+void server_submit(Server* s, PkDev* pk, const uint32_t* w, const uint32_t* rs, uint64_t tag);
+bool server_wait(Server* s, int timeout_ms, uint64_t* tag, bg_proof* out, bg_phase_ms* times, double* latency_ms,
+                 double* queue_ms, int* status);
+size_t server_reserved(Server* s);
 
 }  // namespace bg

@@ -131,6 +131,24 @@ int bg_prove_resident(bg_ctx* ctx, bg_pk* pk, const uint32_t* witness16, const u
  * every result is bit-identical to the same proof made alone. */
 int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnesses16, const uint32_t* const* rs16,
                    size_t count, int lanes, bg_proof* out, bg_phase_ms* times, int* statuses);
+/* Device bytes of scratch one proof against `pk` needs (admission control, capacity planning). */
+size_t bg_prove_footprint(const bg_pk* pk);
+
+/* Serving loop (no counterpart in the reference): `lanes` provers (1..32) take prove requests
+ * from one FIFO queue; the head request starts when a lane is free and the lanes' reserved
+ * scratch stays within hbm_budget_bytes, so requests that arrive while others prove are
+ * admitted as lanes and memory free up and run concurrently (continuous batching).  A request
+ * whose footprint exceeds the budget is refused with BG_E_OOM.  witness16 / rs16 must stay
+ * valid until the request completes.  bg_server_wait returns one completed request (BG_OK) or
+ * BG_E_TIMEOUT; latency_ms is submit -> result, queue_ms submit -> start.  Destroying the
+ * server finishes requests in flight and drops queued ones.  Keys must belong to ctx. */
+typedef struct bg_server bg_server;
+int bg_server_create(bg_ctx* ctx, int lanes, size_t hbm_budget_bytes, bg_server** out);
+int bg_server_submit(bg_server* server, bg_pk* pk, const uint32_t* witness16, const uint32_t* rs16, uint64_t tag);
+int bg_server_wait(bg_server* server, int timeout_ms, uint64_t* tag, bg_proof* out, bg_phase_ms* times,
+                   double* latency_ms, double* queue_ms, int* status);
+size_t bg_server_reserved_bytes(bg_server* server);
+void bg_server_destroy(bg_server* server);
 /* Proof line text exactly as the reference prints it: "A x y\nB x0 x1 y0 y1\nC x y\n"
  * (canonical big-endian 0x + 64 hex digits, bend2/FORMAT.md:33).  buf needs >= 600 bytes. */
 int bg_proof_format(const bg_proof* proof, char* buf, size_t buf_bytes);
