@@ -24,6 +24,7 @@
 #include "msm.h"
 
 #include <cstring>
+#include <memory>
 #include <mutex>
 
 namespace bg {
@@ -171,14 +172,16 @@ __global__ void k_scatter(const uint32_t* __restrict__ scalars, size_t n, int c,
 // entries, one per thread, so every thread runs exactly K mixed additions whatever the bucket
 // sizes are (one thread per bucket would idle most lanes of a warp on Poisson-sized buckets).
 // A run of entries that covers a whole bucket is written to that bucket; a run cut by a slice
-// boundary is written to the thread's slot 0 (run started in an earlier slice) or slot 1
-// (run continues into a later slice), and k_bucket_fixup sums the pieces.
+// boundary becomes a partial: entry 2t of the partial list if the run started in an earlier
+// slice, entry 2t+1 if it continues into a later one, tagged with its bucket in pbkt (absent
+// entries keep the 0xffffffff the list was cleared to).  The partial list is again ordered by
+// bucket, so k_partial_level folds it the same way, level after level (see bucket_phase).
 template <class F>
 __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__ points,
                                                     const uint32_t* __restrict__ offsets,
                                                     const uint32_t* __restrict__ sorted, uint32_t nbuckets,
                                                     uint32_t K, uint32_t* __restrict__ buckets,
-                                                    uint32_t* __restrict__ slot0, uint32_t* __restrict__ slot1) {
+                                                    uint32_t* __restrict__ parts, uint32_t* __restrict__ pbkt) {
   constexpr int FW = FieldWords<F>::value;
   constexpr int PW = 4 * FW;
   const uint32_t total = offsets[nbuckets];
@@ -205,10 +208,13 @@ __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__
     if (code >> 31) p = affine_neg(p);
     acc = xyzz_madd(acc, p);
     if (e + 1 == bend || e + 1 == end) {
-      uint32_t* dst = (bstart < beg) ? slot0 + (size_t)t * PW
-                      : (bend > end) ? slot1 + (size_t)t * PW
-                                     : buckets + (size_t)b * PW;
-      store_xyzz(dst, acc);
+      if (bstart < beg || bend > end) {
+        const size_t slot = 2 * (size_t)t + (bstart < beg ? 0 : 1);
+        store_xyzz(parts + slot * PW, acc);
+        pbkt[slot] = b;
+      } else {
+        store_xyzz(buckets + (size_t)b * PW, acc);
+      }
       acc = xyzz_inf<F>();
       if (e + 1 < end) {
         do {
@@ -221,26 +227,138 @@ __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__
   }
 }
 
-// One thread per bucket: empty buckets become infinity; a bucket cut by slice boundaries is
-// the sum of slot1 of its first slice and slot0 of every later slice it reaches.
+// Slice sizes of the partial-folding levels: level 0 is the accumulation (K entries per
+// thread); level l >= 1 folds kLevelSlice[l] partials per thread.
+constexpr int kMaxLevels = 24;
+struct LevelSlices {
+  uint32_t K[kMaxLevels];  // K[0] = accumulation slice, K[l] = slice of level l
+};
+
+// Range of bucket b's partials in the level-l list: at level 0 its entries [offsets[b],
+// offsets[b+1]); each level maps a range [a, z] cut by slices of size K to
+// [2 floor(a/K) + 1, 2 floor(z/K)] (the first slice's "continues" slot to the last slice's
+// "started earlier" slot).  A range inside one slice is complete at that level.
+BG_DEV void partial_range(const uint32_t* __restrict__ offsets, uint32_t b, int level, const LevelSlices& ks,
+                          uint32_t& a, uint32_t& z) {
+  a = offsets[b];
+  z = offsets[b + 1] - 1;
+  for (int j = 0; j < level; j++) {
+    a = 2 * (a / ks.K[j]) + 1;
+    z = 2 * (z / ks.K[j]);
+  }
+}
+
+// One folding level: thread u sums the runs of equal bucket among partials
+// [u K, (u+1) K) of the level's list; a bucket whose whole range lies in the slice is
+// written to its bucket, otherwise the run becomes entry 2u / 2u+1 of the next list.
 template <class F>
-__global__ void __launch_bounds__(128) k_bucket_fixup(const uint32_t* __restrict__ offsets, uint32_t nbuckets,
-                                                      uint32_t K, const uint32_t* __restrict__ slot0,
-                                                      const uint32_t* __restrict__ slot1,
-                                                      uint32_t* __restrict__ buckets) {
+__global__ void __launch_bounds__(128) k_partial_level(const uint32_t* __restrict__ offsets,
+                                                       const uint32_t* __restrict__ in,
+                                                       const uint32_t* __restrict__ in_bkt, uint32_t n_in,
+                                                       int level, LevelSlices ks, uint32_t* __restrict__ buckets,
+                                                       uint32_t* __restrict__ out, uint32_t* __restrict__ out_bkt) {
+  constexpr int PW = 4 * FieldWords<F>::value;
+  const uint32_t K = ks.K[level];
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t beg64 = (uint64_t)u * K;
+  if (beg64 >= n_in) return;
+  const uint32_t beg = (uint32_t)beg64;
+  const uint32_t end = (n_in - beg) < K ? n_in : beg + K;
+  uint32_t cur = 0xffffffffu;
+  XYZZ<F> acc = xyzz_inf<F>();
+  for (uint32_t e = beg; e <= end; e++) {
+    const uint32_t b = e < end ? in_bkt[e] : 0xffffffffu;
+    if (e < end && b == 0xffffffffu) continue;  // absent slot
+    if (b != cur || e == end) {
+      if (cur != 0xffffffffu) {
+        uint32_t a, z;
+        partial_range(offsets, cur, level, ks, a, z);
+        if (a >= beg && z < end) {
+          store_xyzz(buckets + (size_t)cur * PW, acc);
+        } else {
+          const size_t slot = 2 * (size_t)u + (a < beg ? 0 : 1);
+          store_xyzz(out + slot * PW, acc);
+          out_bkt[slot] = cur;
+        }
+      }
+      if (e == end) break;
+      cur = b;
+      acc = load_xyzz<F>(in + (size_t)e * PW);
+    } else {
+      acc = xyzz_add(acc, load_xyzz<F>(in + (size_t)e * PW));
+    }
+  }
+}
+
+// empty buckets hold infinity (no run writes them)
+template <class F>
+__global__ void k_bucket_empty(const uint32_t* __restrict__ offsets, uint32_t nbuckets,
+                               uint32_t* __restrict__ buckets) {
   constexpr int PW = 4 * FieldWords<F>::value;
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbuckets) return;
-  const uint32_t s = offsets[b], e = offsets[b + 1];
-  if (s == e) {
-    store_xyzz(buckets + (size_t)b * PW, xyzz_inf<F>());
-    return;
+  if (b < nbuckets && offsets[b] == offsets[b + 1]) store_xyzz(buckets + (size_t)b * PW, xyzz_inf<F>());
+}
+
+// Level plan for an accumulation over at most max_entries entries: slice sizes and the
+// partial-list length of every level, ending with a level of one thread.
+struct LevelPlan {
+  LevelSlices ks;
+  int levels = 0;                 // folding levels after the accumulation
+  size_t len[kMaxLevels + 1];     // len[l]: partial-list length entering level l (l >= 1)
+};
+
+inline LevelPlan plan_levels(size_t max_entries, uint32_t K0) {
+  LevelPlan p;
+  p.ks.K[0] = K0;
+  size_t threads = (max_entries + K0 - 1) / K0;
+  int l = 0;
+  while (threads > 1 && l + 1 < kMaxLevels) {
+    l++;
+    p.len[l] = 2 * threads;
+    p.ks.K[l] = l == 1 ? 16 : 8;
+    threads = (p.len[l] + p.ks.K[l] - 1) / p.ks.K[l];
   }
-  const uint32_t tf = s / K, tl = (e - 1) / K;
-  if (tf == tl) return;  // written whole by k_bucket_acc
-  XYZZ<F> acc = load_xyzz<F>(slot1 + (size_t)tf * PW);
-  for (uint32_t t = tf + 1; t <= tl; t++) acc = xyzz_add(acc, load_xyzz<F>(slot0 + (size_t)t * PW));
-  store_xyzz(buckets + (size_t)b * PW, acc);
+  p.levels = l;
+  return p;
+}
+
+// Accumulation and every folding level on `st`; `get(name, words)` supplies scratch
+// (workspace or a fixed array).  After this, buckets[b] holds the sum of bucket b.
+template <class F, class Get>
+void bucket_phase(Ctx* prof, cudaStream_t st, const uint32_t* points, const uint32_t* offsets, const uint32_t* sorted,
+                  uint32_t nkeys, size_t max_entries, uint32_t* buckets, Get get) {
+  constexpr int FW = FieldWords<F>::value;
+  constexpr int PW = 4 * FW;
+  const uint32_t K = FW == 8 ? 32 : 16;
+  const LevelPlan plan = plan_levels(max_entries, K);
+  const size_t threads0 = (max_entries + K - 1) / K;
+  uint32_t* parts[2] = {get("parts0", 2 * threads0 * PW), nullptr};
+  uint32_t* pbkt[2] = {get("pbkt0", 2 * threads0), nullptr};
+  if (plan.levels >= 2) {
+    parts[1] = get("parts1", plan.len[2] * PW);
+    pbkt[1] = get("pbkt1", plan.len[2]);
+  }
+  BG_CUDA(cudaMemsetAsync(pbkt[0], 0xff, 2 * threads0 * sizeof(uint32_t), st));
+  {
+    std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st)
+                                         : nullptr);
+    k_bucket_acc<F><<<ceil_div(threads0, 128), 128, 0, st>>>(points, offsets, sorted, nkeys, K, buckets, parts[0],
+                                                             pbkt[0]);
+    BG_CHECK_LAUNCH();
+  }
+  std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_fixup_g1" : "msm_fixup_g2", st)
+                                       : nullptr);
+  k_bucket_empty<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(offsets, nkeys, buckets);
+  BG_CHECK_LAUNCH();
+  for (int l = 1; l <= plan.levels; l++) {
+    const int src = (l - 1) & 1, dst = l & 1;
+    const size_t n_in = plan.len[l];
+    const size_t threads = (n_in + plan.ks.K[l] - 1) / plan.ks.K[l];
+    if (l < plan.levels) BG_CUDA(cudaMemsetAsync(pbkt[dst], 0xff, 2 * threads * sizeof(uint32_t), st));
+    k_partial_level<F><<<ceil_div(threads, 128), 128, 0, st>>>(offsets, parts[src], pbkt[src], (uint32_t)n_in, l,
+                                                               plan.ks, buckets, parts[dst], pbkt[dst]);
+    BG_CHECK_LAUNCH();
+  }
 }
 
 // Window reduction, one CTA per (window, part).  Part j of window w covers buckets
@@ -348,8 +466,7 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   uint32_t* cursor = ws.get_t<uint32_t>(tag + ".cursor", nkeys + 1);
   uint32_t* sorted = ws.get_t<uint32_t>(tag + ".sorted", max_entries);
   uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", nkeys * PW);
-  uint32_t* slot0 = ws.get_t<uint32_t>(tag + ".slot0", max_threads * PW);
-  uint32_t* slot1 = ws.get_t<uint32_t>(tag + ".slot1", max_threads * PW);
+  (void)max_threads;
 
   BG_CUDA(cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
   {
@@ -364,17 +481,8 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
     k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, cursor, sorted);
     BG_CHECK_LAUNCH();
   }
-  {
-    KernelTimer kt(ctx, FW == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st);
-    k_bucket_acc<F><<<ceil_div(max_threads, 128), 128, 0, st>>>(d_points, offsets, sorted, (uint32_t)nkeys, K,
-                                                                buckets, slot0, slot1);
-    BG_CHECK_LAUNCH();
-  }
-  {
-    KernelTimer kt(ctx, FW == 8 ? "msm_fixup_g1" : "msm_fixup_g2", st);
-    k_bucket_fixup<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(offsets, (uint32_t)nkeys, K, slot0, slot1, buckets);
-    BG_CHECK_LAUNCH();
-  }
+  bucket_phase<F>(ctx.profile ? &ctx : nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets,
+                  [&](const char* name, size_t words) { return ws.get_t<uint32_t>(tag + "." + name, words); });
   plan.entries = max_entries;
 
   // window reduction: RT threads x M buckets x J parts per window
@@ -536,8 +644,11 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   uint32_t* tile_offs = carve(tiles);
   uint32_t* sorted = carve(max_entries);
   uint32_t* buckets = carve(nkeys * PW);
-  uint32_t* slot0 = carve(max_threads * PW);
-  uint32_t* slot1 = carve(max_threads * PW);
+  const LevelPlan lp = plan_levels(max_entries, K);
+  uint32_t* parts0 = carve(2 * max_threads * PW);
+  uint32_t* pbkt0 = carve(2 * max_threads);
+  uint32_t* parts1 = lp.levels >= 2 ? carve(lp.len[2] * PW) : nullptr;
+  uint32_t* pbkt1 = lp.levels >= 2 ? carve(lp.len[2]) : nullptr;
   uint32_t* parts = carve((size_t)W * J * 2 * PW);
   const size_t host_words = (size_t)W * J * 2 * PW;
   if (off > kNoAllocScratchBytes || host_words > kNoAllocHostWords || tiles > (unsigned)kScanTile)
@@ -562,11 +673,11 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   BG_CUDA(cudaMemcpyAsync(cursor, offsets, (nkeys + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
   k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, cursor, sorted);
   BG_CHECK_LAUNCH();
-  k_bucket_acc<Fq><<<ceil_div(max_threads, 128), 128, 0, st>>>(d_points, offsets, sorted, (uint32_t)nkeys, K,
-                                                               buckets, slot0, slot1);
-  BG_CHECK_LAUNCH();
-  k_bucket_fixup<Fq><<<ceil_div(nkeys, 128), 128, 0, st>>>(offsets, (uint32_t)nkeys, K, slot0, slot1, buckets);
-  BG_CHECK_LAUNCH();
+  bucket_phase<Fq>(nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets,
+                   [&](const char* name, size_t) -> uint32_t* {  // the pieces carved above
+                     const std::string s(name);
+                     return s == "parts0" ? parts0 : s == "pbkt0" ? pbkt0 : s == "parts1" ? parts1 : pbkt1;
+                   });
   k_window_reduce<Fq><<<W * J, RT, RT * PW * sizeof(uint32_t), st>>>(buckets, nb, M, J, parts);
   BG_CHECK_LAUNCH();
   BG_CUDA(cudaMemcpyAsync(g_noalloc_host_parts, parts, host_words * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));

@@ -138,3 +138,21 @@ def test_msm_g2_dlog_identity(ctx, log2n):
     got = g2_from_jac_wire(ctx.msm_g2(pts, scalars_wire(sc), n))
     want = o.G2.mul(o.G2.gen, sum(a * b for a, b in zip(ks, sc)) % o.P_FR)
     assert got == want
+
+
+@pytest.mark.parametrize("curve", [bendg.CURVE_G1, bendg.CURVE_G2])
+def test_msm_heavy_buckets(ctx, curve):
+    """scalars from {1, 2, r - 1}: a few buckets receive thousands of entries each, cut into
+    hundreds of slices that the hierarchical partial folding must join"""
+    n = 1 << 15 if curve == bendg.CURVE_G1 else 1 << 12
+    rng = np.random.default_rng(31 + curve)
+    ks = [int.from_bytes(rng.bytes(32), "little") % o.P_FR for _ in range(n)]
+    pts = gpu_points(ctx, curve, ks)
+    choices = [1, 2, o.P_FR - 1]
+    sc = [choices[int(v)] for v in rng.integers(0, 3, size=n)]
+    c = o.G1 if curve == bendg.CURVE_G1 else o.G2
+    want = c.mul(c.gen, sum(a * b for a, b in zip(ks, sc)) % o.P_FR)
+    if curve == bendg.CURVE_G1:
+        assert g1_from_jac_wire(ctx.msm_g1(pts, scalars_wire(sc), n)) == want
+    else:
+        assert g2_from_jac_wire(ctx.msm_g2(pts, scalars_wire(sc), n)) == want
