@@ -395,7 +395,7 @@ int bg_pk_upload(bg_ctx* ctx, const bg_inputs* in, bg_pk** out) {
   *out = nullptr;
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
-    PkDev* pk = pk_upload(ctx->c, *in);
+    PkDev* pk = pk_upload(ctx->c, *in, true);
     *out = new bg_pk{pk, ctx};
   });
 }
@@ -496,7 +496,7 @@ int bg_prove_host(bg_ctx* ctx, const bg_inputs* in, bg_proof* out, bg_phase_ms* 
     const auto t0 = std::chrono::steady_clock::now();
     const Header h = parse_header(*in);
     validate_inputs(*in, h, true);
-    PkDev* pk = pk_upload(ctx->c, *in);
+    PkDev* pk = pk_upload(ctx->c, *in, false);
     const double up_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     try {
       prove_resident(ctx->c, *pk, static_cast<const uint32_t*>(in->witness), static_cast<const uint32_t*>(in->rs),
@@ -534,7 +534,7 @@ int bg_prove_dir(bg_ctx* ctx, const char* dir, bg_proof* out, bg_phase_ms* times
     cudaSetDevice(ctx->c.device);
     const Header h = parse_header(in);
     validate_inputs(in, h, true);
-    PkDev* pk = pk_upload(ctx->c, in);
+    PkDev* pk = pk_upload(ctx->c, in, false);
     const double load_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     try {
       prove_resident(ctx->c, *pk, static_cast<const uint32_t*>(in.witness), static_cast<const uint32_t*>(in.rs),

@@ -29,6 +29,13 @@ BG_DEV Fq2 fsqr(const Fq2& a) {
   return {mul_ool(add(a.c0, a.c1), sub(a.c0, a.c1)), mul_ool(dbl(a.c0), a.c1)};
 }
 
+// 1/a (0 -> 0): Fermat in Fq; in Fq2 through the norm a0^2 + a1^2 (bend2/src/fq2.bend:46-50)
+BG_DEV Fq field_inv_any(const Fq& a) { return inv(a); }
+BG_DEV Fq2 field_inv_any(const Fq2& a) {
+  const Fq ni = inv(add(fsqr(a.c0), fsqr(a.c1)));
+  return {fmul(a.c0, ni), neg(fmul(a.c1, ni))};
+}
+
 template <class F>
 struct Affine {
   F x, y;

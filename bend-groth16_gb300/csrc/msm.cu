@@ -128,7 +128,10 @@ BG_DEV uint32_t signed_digit(const uint32_t* s, int w, int c, uint32_t& carry, b
   return d;
 }
 
-__global__ void k_digits_hist(const uint32_t* __restrict__ scalars, size_t n, int c, int W,
+// Bucket key of window w's digit: w * key_stride + |d| - 1 (key_stride = 2^(c-1): one bucket
+// set per window; 0: all windows share one set).  Point index stored with it:
+// i + w * idx_stride (0: the point itself; n: row w of a table of 2^(c w)-multiples).
+__global__ void k_digits_hist(const uint32_t* __restrict__ scalars, size_t n, int c, int W, uint32_t key_stride,
                               uint32_t* __restrict__ counts, uint32_t* __restrict__ status) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -138,31 +141,56 @@ __global__ void k_digits_hist(const uint32_t* __restrict__ scalars, size_t n, in
     atomicOr(status, BG_DSTATUS_SCALAR_RANGE);
     return;
   }
-  const uint32_t nb = 1u << (c - 1);
   uint32_t carry = 0;
   for (int w = 0; w < W; w++) {
     bool ng;
     const uint32_t mag = signed_digit(s, w, c, carry, ng);
-    if (mag) atomicAdd(&counts[(size_t)w * nb + mag - 1], 1u);
+    if (mag) atomicAdd(&counts[(size_t)w * key_stride + mag - 1], 1u);
   }
 }
 
-__global__ void k_scatter(const uint32_t* __restrict__ scalars, size_t n, int c, int W,
-                          uint32_t* __restrict__ cursor, uint32_t* __restrict__ sorted) {
+__global__ void k_scatter(const uint32_t* __restrict__ scalars, size_t n, int c, int W, uint32_t key_stride,
+                          uint32_t idx_stride, uint32_t* __restrict__ cursor, uint32_t* __restrict__ sorted) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t s[8];
   load_scalar(s, scalars, i);
   if (s[7] >> 30) return;
-  const uint32_t nb = 1u << (c - 1);
   uint32_t carry = 0;
   for (int w = 0; w < W; w++) {
     bool ng;
     const uint32_t mag = signed_digit(s, w, c, carry, ng);
     if (mag) {
-      const uint32_t slot = atomicAdd(&cursor[(size_t)w * nb + mag - 1], 1u);
-      sorted[slot] = (uint32_t)i | (ng ? 0x80000000u : 0u);
+      const uint32_t slot = atomicAdd(&cursor[(size_t)w * key_stride + mag - 1], 1u);
+      sorted[slot] = ((uint32_t)i + (uint32_t)w * idx_stride) | (ng ? 0x80000000u : 0u);
     }
+  }
+}
+
+// Window table of a fixed point set: row w holds 2^(c w) P_i (affine, row-major, n points per
+// row); computed once per proving key, one thread per point (c doublings per row, one
+// inversion per entry).
+template <class F>
+__global__ void __launch_bounds__(128) k_build_table(const uint32_t* __restrict__ pts, size_t n, int c, int W,
+                                                     uint32_t* __restrict__ table) {
+  constexpr int PW = 2 * FieldWords<F>::value;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Affine<F> p = load_affine<F>(pts + i * PW);
+  store_affine(table + i * PW, p);
+  XYZZ<F> q = xyzz_from_affine(p);
+  for (int w = 1; w < W; w++) {
+    for (int d = 0; d < c; d++) q = xyzz_dbl(q);
+    Affine<F> a;
+    if (is_inf(q)) {
+      a.x = field_zero<F>();
+      a.y = field_zero<F>();
+    } else {
+      const F t = field_inv_any(fmul(q.zz, q.zzz));
+      a.x = fmul(q.x, fmul(t, q.zzz));
+      a.y = fmul(q.y, fmul(t, q.zz));
+    }
+    store_affine(table + ((size_t)w * n + i) * PW, a);
   }
 }
 
@@ -441,7 +469,7 @@ constexpr uint32_t kSlice = FieldWords<F>::value == 8 ? 32 : 16;
 
 template <class F>
 void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
-                const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce) {
+                const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce, const MsmTable* table) {
   constexpr int FW = FieldWords<F>::value;
   constexpr int PW = 4 * FW;
   if (n == 0) {
@@ -449,15 +477,21 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
     return;
   }
   if (n >= 0x80000000ull) throw Error(BG_E_ARG, "msm: n must be below 2^31");
+  if (table && table->n != n) throw Error(BG_E_ARG, "msm: window table built for another size");
   msm_init_kernels();
-  const int c = plan.c > 0 ? plan.c : msm_pick_c(n);
+  const int c = table ? table->c : (plan.c > 0 ? plan.c : msm_pick_c(n));
   const int W = 254 / c + 1;
   const uint32_t nb = 1u << (c - 1);
-  const size_t nkeys = (size_t)W * nb;
+  const int sets = table ? 1 : W;  // bucket sets
+  const size_t nkeys = (size_t)sets * nb;
+  const uint32_t key_stride = table ? 0u : nb;
+  const uint32_t idx_stride = table ? (uint32_t)n : 0u;
+  if (table) d_points = table->d;
   plan.c = c;
-  plan.W = W;
+  plan.W = sets;
   const uint32_t K = kSlice<F>;
   const size_t max_entries = n * (size_t)W;
+  if (max_entries >= 0x80000000ull) throw Error(BG_E_ARG, "msm: n x windows must be below 2^31");
   const size_t max_threads = (max_entries + K - 1) / K;
 
   Workspace& ws = ctx.ws;
@@ -471,14 +505,14 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   BG_CUDA(cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
   {
     KernelTimer kt(ctx, "msm_digits", st);
-    k_digits_hist<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, counts, ctx.d_status);
+    k_digits_hist<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, key_stride, counts, ctx.d_status);
     BG_CHECK_LAUNCH();
   }
   exclusive_scan(ws, tag, counts, offsets, nkeys + 1, st, 0);
   BG_CUDA(cudaMemcpyAsync(cursor, offsets, (nkeys + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
   {
     KernelTimer kt(ctx, "msm_scatter", st);
-    k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, cursor, sorted);
+    k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, key_stride, idx_stride, cursor, sorted);
     BG_CHECK_LAUNCH();
   }
   bucket_phase<F>(ctx.profile ? &ctx : nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets,
@@ -489,7 +523,7 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   const uint32_t RT = nb < 256 ? nb : 256;
   const uint32_t M = (nb / RT) < 16 ? nb / RT : 16;
   const uint32_t J = nb / (RT * M);
-  uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)W * J * 2 * PW);
+  uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)sets * J * 2 * PW);
   cudaStream_t rs = st;
   if (st_reduce && st_reduce != st) {
     // the latency-bound reduction runs on its own stream and overlaps whatever `st` does next
@@ -500,15 +534,48 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   }
   {
     KernelTimer kt(ctx, FW == 8 ? "msm_reduce_g1" : "msm_reduce_g2", rs);
-    k_window_reduce<F><<<W * J, RT, RT * PW * sizeof(uint32_t), rs>>>(buckets, nb, M, J, parts);
+    k_window_reduce<F><<<sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(buckets, nb, M, J, parts);
     BG_CHECK_LAUNCH();
   }
   plan.fetch_stream = rs;
   plan.J = J;
   plan.part_span = RT * M;
   plan.d_window_sums = parts;
-  plan.host_window_sums = ctx.host_cache.get_t<uint32_t>(tag + ".window_sums", (size_t)W * J * 2 * PW);
+  plan.host_window_sums = ctx.host_cache.get_t<uint32_t>(tag + ".window_sums", (size_t)sets * J * 2 * PW);
 }
+
+int msm_pick_c_table(size_t n) {
+  // one shared bucket set: wider windows (fewer additions) at the price of 2^(c-1) buckets
+  int lg = 0;
+  while ((size_t(1) << (lg + 1)) <= n) lg++;
+  int c = lg - 1;
+  if (c < 6) c = 6;
+  if (c > 18) c = 18;
+  return c;
+}
+
+template <class F>
+void msm_build_table(cudaStream_t st, const uint32_t* d_points, size_t n, MsmTable& t) {
+  constexpr int PW = 2 * FieldWords<F>::value;
+  t.n = n;
+  t.c = msm_pick_c_table(n);
+  t.W = 254 / t.c + 1;
+  if (n == 0) return;
+  if (n * (size_t)t.W >= 0x80000000ull) throw Error(BG_E_ARG, "msm table: n x windows must be below 2^31");
+  void* p = nullptr;
+  const size_t bytes = n * (size_t)t.W * PW * sizeof(uint32_t);
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(BG_E_OOM, "window table allocation of " + std::to_string(bytes) + " bytes failed");
+  }
+  t.d = static_cast<uint32_t*>(p);
+  k_build_table<F><<<ceil_div(n, 128), 128, 0, st>>>(d_points, n, t.c, t.W, t.d);
+  BG_CHECK_LAUNCH();
+}
+
+template void msm_build_table<Fq>(cudaStream_t, const uint32_t*, size_t, MsmTable&);
+template void msm_build_table<Fq2>(cudaStream_t, const uint32_t*, size_t, MsmTable&);
 
 template <class F>
 void msm_fetch(cudaStream_t st, MsmPlan& plan) {
@@ -551,9 +618,9 @@ void msm_init_kernels() {
 }
 
 template void msm_launch<Fq>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const uint32_t*, size_t,
-                             MsmPlan&, cudaStream_t);
+                             MsmPlan&, cudaStream_t, const MsmTable*);
 template void msm_launch<Fq2>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const uint32_t*, size_t,
-                              MsmPlan&, cudaStream_t);
+                              MsmPlan&, cudaStream_t, const MsmTable*);
 template void msm_fetch<Fq>(cudaStream_t, MsmPlan&);
 template void msm_fetch<Fq2>(cudaStream_t, MsmPlan&);
 template void msm_finish<Fq>(const MsmPlan&, uint32_t*);
@@ -657,7 +724,7 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   // what must start at zero: the status word and the bucket counters
   BG_CUDA(cudaMemsetAsync(status, 0, sizeof(uint32_t), st));
   BG_CUDA(cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
-  k_digits_hist<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, counts, status);
+  k_digits_hist<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, nb, counts, status);
   BG_CHECK_LAUNCH();
   if (tiles == 1) {
     k_scan_tile<<<1, kScanThreads, 0, st>>>(counts, offsets, nullptr, nkeys + 1);
@@ -671,7 +738,7 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
     BG_CHECK_LAUNCH();
   }
   BG_CUDA(cudaMemcpyAsync(cursor, offsets, (nkeys + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
-  k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, cursor, sorted);
+  k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, nb, 0, cursor, sorted);
   BG_CHECK_LAUNCH();
   bucket_phase<Fq>(nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets,
                    [&](const char* name, size_t) -> uint32_t* {  // the pieces carved above

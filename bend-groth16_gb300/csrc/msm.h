@@ -20,17 +20,31 @@ struct MsmPlan {
   uint32_t* host_window_sums = nullptr;
 };
 
+// Window table of a fixed point set: row w (w < W) holds 2^(c w) P_i for all i, so every
+// window's digits index one shared bucket set (no window combination afterwards).
+struct MsmTable {
+  uint32_t* d = nullptr;  // W rows of n packed affine points (device, owned by the key)
+  size_t n = 0;
+  int c = 0, W = 0;
+};
+
 int msm_pick_c(size_t n);
+int msm_pick_c_table(size_t n);
 void msm_init_kernels();
+// allocate t.d (cudaMalloc) and fill it from n packed affine points on `st`
+template <class F>
+void msm_build_table(cudaStream_t st, const uint32_t* d_points, size_t n, MsmTable& t);
 void exclusive_scan(Workspace& ws, const std::string& tag, const uint32_t* d_in, uint32_t* d_out, size_t n,
                     cudaStream_t st, int depth);
 
 // Enqueue every device phase of one MSM on `st` (the window reduction on `st_reduce` when
 // given, after an event); scratch buffers are named by `tag` so that MSMs in flight at the
 // same time use different memory.
+// With `table`, d_points is ignored and the table's rows are used (one bucket set).
 template <class F>
 void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
-                const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce = nullptr);
+                const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce = nullptr,
+                const MsmTable* table = nullptr);
 // Enqueue the copy of the window sums to the host.
 template <class F>
 void msm_fetch(cudaStream_t st, MsmPlan& plan);

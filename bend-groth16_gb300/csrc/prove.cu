@@ -236,7 +236,7 @@ void check_status(Ctx& ctx, cudaStream_t st) {
   }
 }
 
-PkDev* pk_upload(Ctx& ctx, const bg_inputs& in) {
+PkDev* pk_upload(Ctx& ctx, const bg_inputs& in, bool build_tables) {
   const Header h = parse_header(in);
   validate_inputs(in, h, false);
   PkDev* pk = new PkDev();
@@ -258,6 +258,14 @@ PkDev* pk_upload(Ctx& ctx, const bg_inputs& in) {
     pk->delta = host_affine_from_wire<FqOps>(g1 + 64);
     pk->beta2 = host_affine_from_wire<Fq2Ops>(g2);
     pk->delta2 = host_affine_from_wire<Fq2Ops>(g2 + 64);
+    if (build_tables) {
+      msm_build_table<Fq>(st, pk->pa, h.na, pk->tab[0]);
+      msm_build_table<Fq>(st, pk->pb1, h.nb, pk->tab[1]);
+      msm_build_table<Fq2>(st, pk->pb2, h.nb, pk->tab[2]);
+      msm_build_table<Fq>(st, pk->ph, h.nh, pk->tab[3]);
+      msm_build_table<Fq>(st, pk->pl, h.nl, pk->tab[4]);
+      pk->tables = true;
+    }
     check_status(ctx, st);
   } catch (...) {
     pk_free(pk);
@@ -271,6 +279,8 @@ void pk_free(PkDev* pk) {
   for (uint32_t* p : {pk->pa, pk->pb1, pk->pb2, pk->ph, pk->pl, pk->ca.offs, pk->ca.cols, pk->ca.coeffs,
                       pk->cb.offs, pk->cb.cols, pk->cb.coeffs, pk->cc.offs, pk->cc.cols, pk->cc.coeffs})
     if (p) cudaFree(p);
+  for (MsmTable& t : pk->tab)
+    if (t.d) cudaFree(t.d);
   delete pk;
 }
 
@@ -366,12 +376,14 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     const uint32_t* pts;
     const uint32_t* sc;
     size_t n;
+    const MsmTable* tab;  // the query set's window table (resident keys), else null
   };
-  const Job jobs[5] = {{0, "msm_a", false, pk.pa, zc, h.na},
-                       {1, "msm_b1", false, pk.pb1, zc, h.nb},
-                       {2, "msm_b2", true, pk.pb2, zc, h.nb},
-                       {4, "msm_l", false, pk.pl, zc + 8 * (size_t)h.ni, h.nl},
-                       {3, "msm_h", false, pk.ph, hc, h.nh}};
+  auto tab = [&](int k) -> const MsmTable* { return pk.tables && pk.tab[k].d ? &pk.tab[k] : nullptr; };
+  const Job jobs[5] = {{0, "msm_a", false, pk.pa, zc, h.na, tab(0)},
+                       {1, "msm_b1", false, pk.pb1, zc, h.nb, tab(1)},
+                       {2, "msm_b2", true, pk.pb2, zc, h.nb, tab(2)},
+                       {4, "msm_l", false, pk.pl, zc + 8 * (size_t)h.ni, h.nl, tab(4)},
+                       {3, "msm_h", false, pk.ph, hc, h.nh, tab(3)}};
   cudaStream_t acc_st = ctx.side[0];
   BG_CUDA(cudaStreamWaitEvent(acc_st, ctx.ev_fork, 0));
   for (int j = 0; j < 5; j++) {
@@ -381,10 +393,10 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     MsmPlan& p = plan[jb.idx];
     t_msm[jb.idx].start(acc_st);
     if (jb.g2) {
-      msm_launch<Fq2>(ctx, acc_st, jb.tag, jb.pts, jb.sc, jb.n, p, red);
+      msm_launch<Fq2>(ctx, acc_st, jb.tag, jb.pts, jb.sc, jb.n, p, red, jb.tab);
       msm_fetch<Fq2>(acc_st, p);
     } else {
-      msm_launch<Fq>(ctx, acc_st, jb.tag, jb.pts, jb.sc, jb.n, p, red);
+      msm_launch<Fq>(ctx, acc_st, jb.tag, jb.pts, jb.sc, jb.n, p, red, jb.tab);
       msm_fetch<Fq>(acc_st, p);
     }
     t_msm[jb.idx].stop(red);

@@ -2,6 +2,7 @@
 #pragma once
 #include "common.cuh"
 #include "host_ff.hpp"
+#include "msm.h"
 
 namespace bg {
 
@@ -24,11 +25,16 @@ struct PkDev {
   CsrDev ca, cb, cc;
   bgh::Aff<bgh::FqOps> alpha, beta, delta;
   bgh::Aff<bgh::Fq2Ops> beta2, delta2;
+  // window tables of the five query sets (a, b1, b2, h, l), built for resident keys
+  MsmTable tab[5];
+  bool tables = false;
 };
 
 Header parse_header(const bg_inputs& in);
 void validate_inputs(const bg_inputs& in, const Header& h, bool need_witness);
-PkDev* pk_upload(Ctx& ctx, const bg_inputs& in);
+// with build_tables, each query set also gets its 2^(c w) window table (resident keys proving
+// many proofs; a one-shot proof skips them)
+PkDev* pk_upload(Ctx& ctx, const bg_inputs& in, bool build_tables);
 void pk_free(PkDev* pk);
 void check_status(Ctx& ctx, cudaStream_t st);
 void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32_t* rs16, bg_proof* out,
