@@ -150,9 +150,15 @@ void ctx_init(Ctx& c, int device) {
   BG_CUDA(cudaSetDevice(device));
   c.device = device;
   BG_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
-  BG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  // Priorities: the main stream (evaluations, QAP) and the fixup/reduction streams carry the
+  // latency-bound chains of a proof, side[0] the throughput-bound accumulations; when an SM
+  // frees a slot, pending blocks of the higher-priority streams are dispatched first, so the
+  // accumulations fill whatever the chains leave instead of starving them.
+  int least = 0, greatest = 0;
+  BG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  BG_CUDA(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking, greatest));
   for (int i = 0; i < kStreams; i++) {
-    BG_CUDA(cudaStreamCreateWithFlags(&c.side[i], cudaStreamNonBlocking));
+    BG_CUDA(cudaStreamCreateWithPriority(&c.side[i], cudaStreamNonBlocking, i == 0 ? least : greatest));
     BG_CUDA(cudaEventCreateWithFlags(&c.ev_join[i], cudaEventDisableTiming));
   }
   BG_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));

@@ -201,15 +201,15 @@ __global__ void __launch_bounds__(128) k_build_table(const uint32_t* __restrict_
 // sizes are (one thread per bucket would idle most lanes of a warp on Poisson-sized buckets).
 // A run of entries that covers a whole bucket is written to that bucket; a run cut by a slice
 // boundary becomes a partial: entry 2t of the partial list if the run started in an earlier
-// slice, entry 2t+1 if it continues into a later one, tagged with its bucket in pbkt (absent
-// entries keep the 0xffffffff the list was cleared to).  The partial list is again ordered by
-// bucket, so k_partial_level folds it the same way, level after level (see bucket_phase).
+// slice, entry 2t+1 if the bucket starts in slice t and continues into a later one.  owner[t]
+// names that bucket (0xffffffff when slice t ends on a bucket boundary), so a bucket cut into
+// slices t0..t1 has its partials at 2 t0 + 1 and 2 t for t0 < t <= t1 (k_bucket_fixup).
 template <class F>
 __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__ points,
                                                     const uint32_t* __restrict__ offsets,
                                                     const uint32_t* __restrict__ sorted, uint32_t nbuckets,
                                                     uint32_t K, uint32_t* __restrict__ buckets,
-                                                    uint32_t* __restrict__ parts, uint32_t* __restrict__ pbkt) {
+                                                    uint32_t* __restrict__ parts, uint32_t* __restrict__ owner) {
   constexpr int FW = FieldWords<F>::value;
   constexpr int PW = 4 * FW;
   const uint32_t total = offsets[nbuckets];
@@ -229,6 +229,7 @@ __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__
   // step; a bucket boundary only costs a short divergent flush.
   uint32_t b = lo;
   uint32_t bstart = offsets[b], bend = offsets[b + 1];
+  uint32_t continues = 0xffffffffu;
   XYZZ<F> acc = xyzz_inf<F>();
   for (uint32_t e = beg; e < end; e++) {
     const uint32_t code = sorted[e];
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__
       if (bstart < beg || bend > end) {
         const size_t slot = 2 * (size_t)t + (bstart < beg ? 0 : 1);
         store_xyzz(parts + slot * PW, acc);
-        pbkt[slot] = b;
+        if (bstart >= beg) continues = b;
       } else {
         store_xyzz(buckets + (size_t)b * PW, acc);
       }
@@ -253,140 +254,143 @@ __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__
       }
     }
   }
+  owner[t] = continues;
 }
 
-// Slice sizes of the partial-folding levels: level 0 is the accumulation (K entries per
-// thread); level l >= 1 folds kLevelSlice[l] partials per thread.
-constexpr int kMaxLevels = 24;
-struct LevelSlices {
-  uint32_t K[kMaxLevels];  // K[0] = accumulation slice, K[l] = slice of level l
-};
+// Buckets cut by slice boundaries.  Thread t serves the bucket that starts in slice t and
+// continues (owner[t]); its partials are entry 2t + 1 and entries 2u for t < u <= t1, t1 the
+// slice of the bucket's last entry.  Up to kFixupChain further partials are added here, one
+// chain per cut bucket (most buckets span two or three slices); a bucket spanning more slices
+// is listed in heavy[1 + i] (heavy[0] counts them) for k_bucket_heavy.
+constexpr uint32_t kFixupChain = 8;
 
-// Range of bucket b's partials in the level-l list: at level 0 its entries [offsets[b],
-// offsets[b+1]); each level maps a range [a, z] cut by slices of size K to
-// [2 floor(a/K) + 1, 2 floor(z/K)] (the first slice's "continues" slot to the last slice's
-// "started earlier" slot).  A range inside one slice is complete at that level.
-BG_DEV void partial_range(const uint32_t* __restrict__ offsets, uint32_t b, int level, const LevelSlices& ks,
-                          uint32_t& a, uint32_t& z) {
-  a = offsets[b];
-  z = offsets[b + 1] - 1;
-  for (int j = 0; j < level; j++) {
-    a = 2 * (a / ks.K[j]) + 1;
-    z = 2 * (z / ks.K[j]);
-  }
-}
-
-// One folding level: thread u sums the runs of equal bucket among partials
-// [u K, (u+1) K) of the level's list; a bucket whose whole range lies in the slice is
-// written to its bucket, otherwise the run becomes entry 2u / 2u+1 of the next list.
 template <class F>
-__global__ void __launch_bounds__(128) k_partial_level(const uint32_t* __restrict__ offsets,
-                                                       const uint32_t* __restrict__ in,
-                                                       const uint32_t* __restrict__ in_bkt, uint32_t n_in,
-                                                       int level, LevelSlices ks, uint32_t* __restrict__ buckets,
-                                                       uint32_t* __restrict__ out, uint32_t* __restrict__ out_bkt) {
+__global__ void __launch_bounds__(128) k_bucket_fixup(const uint32_t* __restrict__ offsets, uint32_t nbuckets,
+                                                      const uint32_t* __restrict__ parts,
+                                                      const uint32_t* __restrict__ owner, uint32_t K,
+                                                      uint32_t* __restrict__ buckets, uint32_t* __restrict__ heavy) {
   constexpr int PW = 4 * FieldWords<F>::value;
-  const uint32_t K = ks.K[level];
-  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint64_t beg64 = (uint64_t)u * K;
-  if (beg64 >= n_in) return;
-  const uint32_t beg = (uint32_t)beg64;
-  const uint32_t end = (n_in - beg) < K ? n_in : beg + K;
-  uint32_t cur = 0xffffffffu;
-  XYZZ<F> acc = xyzz_inf<F>();
-  for (uint32_t e = beg; e <= end; e++) {
-    const uint32_t b = e < end ? in_bkt[e] : 0xffffffffu;
-    if (e < end && b == 0xffffffffu) continue;  // absent slot
-    if (b != cur || e == end) {
-      if (cur != 0xffffffffu) {
-        uint32_t a, z;
-        partial_range(offsets, cur, level, ks, a, z);
-        if (a >= beg && z < end) {
-          store_xyzz(buckets + (size_t)cur * PW, acc);
-        } else {
-          const size_t slot = 2 * (size_t)u + (a < beg ? 0 : 1);
-          store_xyzz(out + slot * PW, acc);
-          out_bkt[slot] = cur;
-        }
-      }
-      if (e == end) break;
-      cur = b;
-      acc = load_xyzz<F>(in + (size_t)e * PW);
-    } else {
-      acc = xyzz_add(acc, load_xyzz<F>(in + (size_t)e * PW));
-    }
+  const uint32_t total = offsets[nbuckets];
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((uint64_t)t * K >= total) return;
+  const uint32_t b = owner[t];
+  if (b == 0xffffffffu) return;
+  const uint32_t t1 = (offsets[b + 1] - 1) / K;
+  if (t1 - t > kFixupChain) {
+    heavy[1 + atomicAdd(heavy, 1u)] = t;
+    return;
   }
+  XYZZ<F> acc = load_xyzz<F>(parts + (2 * (size_t)t + 1) * PW);
+  for (uint32_t u = t + 1; u <= t1; u++) acc = xyzz_add(acc, load_xyzz<F>(parts + 2 * (size_t)u * PW));
+  store_xyzz(buckets + (size_t)b * PW, acc);
 }
 
-// empty buckets hold infinity (no run writes them)
+// Heavy buckets (more than kFixupChain + 1 partials): one CTA per bucket, a strided sum per
+// thread and a tree over the CTA.  The grid is fixed; CTAs loop over however many the fixup
+// listed (none for uniformly spread scalars).
+template <class F>
+__global__ void __launch_bounds__(128) k_bucket_heavy(const uint32_t* __restrict__ offsets,
+                                                      const uint32_t* __restrict__ parts,
+                                                      const uint32_t* __restrict__ owner, uint32_t K,
+                                                      const uint32_t* __restrict__ heavy,
+                                                      uint32_t* __restrict__ buckets) {
+  constexpr int PW = 4 * FieldWords<F>::value;
+  extern __shared__ uint32_t sm[];
+  const uint32_t nh = heavy[0];
+  for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+    const uint32_t t0 = heavy[1 + h];
+    const uint32_t b = owner[t0];
+    const uint32_t np = (offsets[b + 1] - 1) / K - t0 + 1;
+    XYZZ<F> acc = xyzz_inf<F>();
+    for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
+      const size_t slot = i == 0 ? 2 * (size_t)t0 + 1 : 2 * ((size_t)t0 + i);
+      acc = xyzz_add(acc, load_xyzz<F>(parts + slot * PW));
+    }
+    store_xyzz(sm + (size_t)threadIdx.x * PW, acc);
+    __syncthreads();
+    for (uint32_t d = blockDim.x >> 1; d >= 1; d >>= 1) {
+      if (threadIdx.x < d) {
+        acc = xyzz_add(acc, load_xyzz<F>(sm + (size_t)(threadIdx.x + d) * PW));
+        store_xyzz(sm + (size_t)threadIdx.x * PW, acc);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) store_xyzz(buckets + (size_t)b * PW, acc);
+    __syncthreads();
+  }
+}
+constexpr uint32_t kHeavyThreads = 128;
+constexpr uint32_t kHeavyGrid = 152;
+
+// empty buckets hold infinity (no run writes them); also clears the heavy-bucket count
 template <class F>
 __global__ void k_bucket_empty(const uint32_t* __restrict__ offsets, uint32_t nbuckets,
-                               uint32_t* __restrict__ buckets) {
+                               uint32_t* __restrict__ buckets, uint32_t* __restrict__ heavy) {
   constexpr int PW = 4 * FieldWords<F>::value;
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b == 0) heavy[0] = 0;
   if (b < nbuckets && offsets[b] == offsets[b + 1]) store_xyzz(buckets + (size_t)b * PW, xyzz_inf<F>());
 }
 
-// Level plan for an accumulation over at most max_entries entries: slice sizes and the
-// partial-list length of every level, ending with a level of one thread.
-struct LevelPlan {
-  LevelSlices ks;
-  int levels = 0;                 // folding levels after the accumulation
-  size_t len[kMaxLevels + 1];     // len[l]: partial-list length entering level l (l >= 1)
-};
+// entries per accumulation thread (the fixup adds one point per slice boundary, 1/32 of the
+// accumulation's additions)
+template <class F>
+constexpr uint32_t kSlice = 32;
 
-inline LevelPlan plan_levels(size_t max_entries, uint32_t K0) {
-  LevelPlan p;
-  p.ks.K[0] = K0;
-  size_t threads = (max_entries + K0 - 1) / K0;
-  int l = 0;
-  while (threads > 1 && l + 1 < kMaxLevels) {
-    l++;
-    p.len[l] = 2 * threads;
-    p.ks.K[l] = l == 1 ? 16 : 8;
-    threads = (p.len[l] + p.ks.K[l] - 1) / p.ks.K[l];
-  }
-  p.levels = l;
-  return p;
+// Scratch of the bucket phase for at most max_entries entries (words): partials, owners and
+// the heavy list.
+struct BucketScratch {
+  uint32_t* parts = nullptr;  // 2 x slices XYZZ points
+  uint32_t* owner = nullptr;  // slices
+  uint32_t* heavy = nullptr;  // 1 + slices / kFixupChain + 1
+};
+template <class F>
+inline size_t bucket_slices(size_t max_entries) {
+  return (max_entries + kSlice<F> - 1) / kSlice<F>;
+}
+template <class F, class Get>
+BucketScratch bucket_scratch(size_t max_entries, Get get) {
+  constexpr int PW = 4 * FieldWords<F>::value;
+  const size_t s = bucket_slices<F>(max_entries);
+  BucketScratch b;
+  b.parts = get("parts", 2 * s * PW);
+  b.owner = get("owner", s);
+  b.heavy = get("heavy", s / kFixupChain + 2);
+  return b;
 }
 
-// Accumulation and every folding level on `st`; `get(name, words)` supplies scratch
-// (workspace or a fixed array).  After this, buckets[b] holds the sum of bucket b.
-template <class F, class Get>
-void bucket_phase(Ctx* prof, cudaStream_t st, const uint32_t* points, const uint32_t* offsets, const uint32_t* sorted,
-                  uint32_t nkeys, size_t max_entries, uint32_t* buckets, Get get) {
+// Accumulation on `st`: buckets of single-slice runs are final, cut buckets leave partials.
+template <class F>
+void bucket_accumulate(Ctx* prof, cudaStream_t st, const uint32_t* points, const uint32_t* offsets,
+                       const uint32_t* sorted, uint32_t nkeys, size_t max_entries, uint32_t* buckets,
+                       const BucketScratch& s) {
+  constexpr int FW = FieldWords<F>::value;
+  const size_t slices = bucket_slices<F>(max_entries);
+  std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st)
+                                       : nullptr);
+  k_bucket_acc<F><<<ceil_div(slices, 128), 128, 0, st>>>(points, offsets, sorted, nkeys, kSlice<F>, buckets, s.parts,
+                                                         s.owner);
+  BG_CHECK_LAUNCH();
+}
+
+// Empty buckets, cut buckets and heavy buckets on `st`; afterwards buckets[b] holds the sum
+// of bucket b for every b.
+template <class F>
+void bucket_fixup(Ctx* prof, cudaStream_t st, const uint32_t* offsets, uint32_t nkeys, size_t max_entries,
+                  uint32_t* buckets, const BucketScratch& s) {
   constexpr int FW = FieldWords<F>::value;
   constexpr int PW = 4 * FW;
-  const uint32_t K = FW == 8 ? 32 : 16;
-  const LevelPlan plan = plan_levels(max_entries, K);
-  const size_t threads0 = (max_entries + K - 1) / K;
-  uint32_t* parts[2] = {get("parts0", 2 * threads0 * PW), nullptr};
-  uint32_t* pbkt[2] = {get("pbkt0", 2 * threads0), nullptr};
-  if (plan.levels >= 2) {
-    parts[1] = get("parts1", plan.len[2] * PW);
-    pbkt[1] = get("pbkt1", plan.len[2]);
-  }
-  BG_CUDA(cudaMemsetAsync(pbkt[0], 0xff, 2 * threads0 * sizeof(uint32_t), st));
-  {
-    std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st)
-                                         : nullptr);
-    k_bucket_acc<F><<<ceil_div(threads0, 128), 128, 0, st>>>(points, offsets, sorted, nkeys, K, buckets, parts[0],
-                                                             pbkt[0]);
-    BG_CHECK_LAUNCH();
-  }
+  const size_t slices = bucket_slices<F>(max_entries);
   std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_fixup_g1" : "msm_fixup_g2", st)
                                        : nullptr);
-  k_bucket_empty<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(offsets, nkeys, buckets);
+  k_bucket_empty<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(offsets, nkeys, buckets, s.heavy);
   BG_CHECK_LAUNCH();
-  for (int l = 1; l <= plan.levels; l++) {
-    const int src = (l - 1) & 1, dst = l & 1;
-    const size_t n_in = plan.len[l];
-    const size_t threads = (n_in + plan.ks.K[l] - 1) / plan.ks.K[l];
-    if (l < plan.levels) BG_CUDA(cudaMemsetAsync(pbkt[dst], 0xff, 2 * threads * sizeof(uint32_t), st));
-    k_partial_level<F><<<ceil_div(threads, 128), 128, 0, st>>>(offsets, parts[src], pbkt[src], (uint32_t)n_in, l,
-                                                               plan.ks, buckets, parts[dst], pbkt[dst]);
-    BG_CHECK_LAUNCH();
-  }
+  k_bucket_fixup<F><<<ceil_div(slices, 128), 128, 0, st>>>(offsets, nkeys, s.parts, s.owner, kSlice<F>, buckets,
+                                                           s.heavy);
+  BG_CHECK_LAUNCH();
+  k_bucket_heavy<F><<<kHeavyGrid, kHeavyThreads, kHeavyThreads * PW * sizeof(uint32_t), st>>>(
+      offsets, s.parts, s.owner, kSlice<F>, s.heavy, buckets);
+  BG_CHECK_LAUNCH();
 }
 
 // Window reduction, one CTA per (window, part).  Part j of window w covers buckets
@@ -442,6 +446,23 @@ __global__ void k_window_reduce(const uint32_t* __restrict__ buckets, uint32_t n
   }
 }
 
+// Shape of the window reduction: RT threads x M buckets per thread x J parts per window.
+// With one shared bucket set (window tables) the reduction is the only one of its MSM and its
+// dependent chain (2M additions + two log2(RT) trees) is the tail of the MSM, so it runs with
+// M = 4 and more parts (the host adds J parts in microseconds); with a bucket set per window
+// there are already W x J CTAs and M = 16 keeps the host's share small.
+struct ReduceShape {
+  uint32_t RT, M, J;
+};
+inline ReduceShape reduce_shape(uint32_t nb, int sets) {
+  ReduceShape s;
+  s.RT = nb < 256 ? nb : 256;
+  const uint32_t mmax = sets == 1 ? 4u : 16u;
+  s.M = (nb / s.RT) < mmax ? nb / s.RT : mmax;
+  s.J = nb / (s.RT * s.M);
+  return s;
+}
+
 // ---------------------------------------------------------------- host driver
 int msm_pick_c(size_t n) {
   int lg = 0;
@@ -462,10 +483,6 @@ template <>
 struct HostField<Fq2> {
   typedef bgh::Fq2Ops T;
 };
-
-// entries per accumulation thread
-template <class F>
-constexpr uint32_t kSlice = FieldWords<F>::value == 8 ? 32 : 16;
 
 template <class F>
 void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
@@ -489,10 +506,8 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   if (table) d_points = table->d;
   plan.c = c;
   plan.W = sets;
-  const uint32_t K = kSlice<F>;
   const size_t max_entries = n * (size_t)W;
   if (max_entries >= 0x80000000ull) throw Error(BG_E_ARG, "msm: n x windows must be below 2^31");
-  const size_t max_threads = (max_entries + K - 1) / K;
 
   Workspace& ws = ctx.ws;
   uint32_t* counts = ws.get_t<uint32_t>(tag + ".counts", nkeys + 1);
@@ -500,7 +515,8 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   uint32_t* cursor = ws.get_t<uint32_t>(tag + ".cursor", nkeys + 1);
   uint32_t* sorted = ws.get_t<uint32_t>(tag + ".sorted", max_entries);
   uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", nkeys * PW);
-  (void)max_threads;
+  const BucketScratch bs = bucket_scratch<F>(
+      max_entries, [&](const char* name, size_t words) { return ws.get_t<uint32_t>(tag + ".slice_" + name, words); });
 
   BG_CUDA(cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
   {
@@ -515,23 +531,24 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
     k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, key_stride, idx_stride, cursor, sorted);
     BG_CHECK_LAUNCH();
   }
-  bucket_phase<F>(ctx.profile ? &ctx : nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets,
-                  [&](const char* name, size_t words) { return ws.get_t<uint32_t>(tag + "." + name, words); });
+  Ctx* prof = ctx.profile ? &ctx : nullptr;
+  bucket_accumulate<F>(prof, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets, bs);
   plan.entries = max_entries;
 
-  // window reduction: RT threads x M buckets x J parts per window
-  const uint32_t RT = nb < 256 ? nb : 256;
-  const uint32_t M = (nb / RT) < 16 ? nb / RT : 16;
-  const uint32_t J = nb / (RT * M);
-  uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)sets * J * 2 * PW);
   cudaStream_t rs = st;
   if (st_reduce && st_reduce != st) {
-    // the latency-bound reduction runs on its own stream and overlaps whatever `st` does next
+    // the latency-bound fixup and reduction run on their own stream and overlap whatever `st`
+    // does next (the next MSM's accumulation)
     cudaEvent_t ev = ctx.event(tag + ".acc_done");
     BG_CUDA(cudaEventRecord(ev, st));
     BG_CUDA(cudaStreamWaitEvent(st_reduce, ev, 0));
     rs = st_reduce;
   }
+  bucket_fixup<F>(prof, rs, offsets, (uint32_t)nkeys, max_entries, buckets, bs);
+
+  const ReduceShape rsh = reduce_shape(nb, sets);
+  const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
+  uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)sets * J * 2 * PW);
   {
     KernelTimer kt(ctx, FW == 8 ? "msm_reduce_g1" : "msm_reduce_g2", rs);
     k_window_reduce<F><<<sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(buckets, nb, M, J, parts);
@@ -689,12 +706,9 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   const int W = 254 / c + 1;
   const uint32_t nb = 1u << (c - 1);
   const size_t nkeys = (size_t)W * nb;
-  const uint32_t K = kSlice<Fq>;
   const size_t max_entries = n * (size_t)W;
-  const size_t max_threads = (max_entries + K - 1) / K;
-  const uint32_t RT = nb < 256 ? nb : 256;
-  const uint32_t M = (nb / RT) < 16 ? nb / RT : 16;
-  const uint32_t J = nb / (RT * M);
+  const ReduceShape rsh = reduce_shape(nb, W);
+  const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
   const unsigned tiles = ceil_div(nkeys + 1, kScanTile);
 
   size_t off = 0;
@@ -711,11 +725,7 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   uint32_t* tile_offs = carve(tiles);
   uint32_t* sorted = carve(max_entries);
   uint32_t* buckets = carve(nkeys * PW);
-  const LevelPlan lp = plan_levels(max_entries, K);
-  uint32_t* parts0 = carve(2 * max_threads * PW);
-  uint32_t* pbkt0 = carve(2 * max_threads);
-  uint32_t* parts1 = lp.levels >= 2 ? carve(lp.len[2] * PW) : nullptr;
-  uint32_t* pbkt1 = lp.levels >= 2 ? carve(lp.len[2]) : nullptr;
+  const BucketScratch bs = bucket_scratch<Fq>(max_entries, [&](const char*, size_t words) { return carve(words); });
   uint32_t* parts = carve((size_t)W * J * 2 * PW);
   const size_t host_words = (size_t)W * J * 2 * PW;
   if (off > kNoAllocScratchBytes || host_words > kNoAllocHostWords || tiles > (unsigned)kScanTile)
@@ -740,11 +750,8 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   BG_CUDA(cudaMemcpyAsync(cursor, offsets, (nkeys + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
   k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, nb, 0, cursor, sorted);
   BG_CHECK_LAUNCH();
-  bucket_phase<Fq>(nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets,
-                   [&](const char* name, size_t) -> uint32_t* {  // the pieces carved above
-                     const std::string s(name);
-                     return s == "parts0" ? parts0 : s == "pbkt0" ? pbkt0 : s == "parts1" ? parts1 : pbkt1;
-                   });
+  bucket_accumulate<Fq>(nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets, bs);
+  bucket_fixup<Fq>(nullptr, st, offsets, (uint32_t)nkeys, max_entries, buckets, bs);
   k_window_reduce<Fq><<<W * J, RT, RT * PW * sizeof(uint32_t), st>>>(buckets, nb, M, J, parts);
   BG_CHECK_LAUNCH();
   BG_CUDA(cudaMemcpyAsync(g_noalloc_host_parts, parts, host_words * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));

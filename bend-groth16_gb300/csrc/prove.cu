@@ -470,11 +470,13 @@ static size_t msm_footprint(size_t n, bool g2) {
   if (n == 0) return 0;
   const int c = msm_pick_c(n);
   const size_t W = 254 / c + 1, nb = size_t(1) << (c - 1), nkeys = W * nb;
-  const size_t PW = g2 ? 64 : 32, K = g2 ? 16 : 32;
+  const size_t PW = g2 ? 64 : 32, K = 32;
   const size_t entries = n * W, threads = (entries + K - 1) / K;
   const size_t RT = nb < 256 ? nb : 256, M = (nb / RT) < 16 ? nb / RT : 16, J = nb / (RT * M);
-  const size_t words = 3 * (nkeys + 1) + entries + nkeys * PW + 2 * threads * PW + W * J * 2 * PW +
-                       2 * ((nkeys + 1) / 2048 + 1);
+  // counters, offsets, cursors, entry list, buckets, slice partials + owners + heavy list,
+  // window parts, scan sums
+  const size_t words = 3 * (nkeys + 1) + entries + nkeys * PW + 2 * threads * PW + threads + threads / 8 + 2 +
+                       W * J * 2 * PW + 2 * ((nkeys + 1) / 2048 + 1);
   return words * 4;
 }
 

@@ -97,8 +97,47 @@ def test_prove_matches_c_oracle(ctx, tmp_path, log2n):
     import oracle_c
     path = str(tmp_path / "sq")
     ctx.synth_square_chain(log2n, 4242 + log2n, path)
-    proof, _ = ctx.prove_dir(path)
     want, _ = oracle_c.prove_dir(path)
-    got = np.concatenate([np.ctypeslib.as_array(proof.a), np.ctypeslib.as_array(proof.b),
-                          np.ctypeslib.as_array(proof.c)])
-    assert np.array_equal(got, want)
+    proof, _ = ctx.prove_dir(path)
+    assert np.array_equal(proof_words(proof), want)
+    # the resident key proves through its window tables (one shared bucket set per MSM)
+    files = bendg.HostFiles(path)
+    key = ctx.pk_upload(files)
+    proof, _ = key.prove(files.words("witness"), files.words("rs"))
+    key.release()
+    assert np.array_equal(proof_words(proof), want)
+
+
+def proof_words(proof):
+    return np.concatenate([np.ctypeslib.as_array(proof.a), np.ctypeslib.as_array(proof.b),
+                           np.ctypeslib.as_array(proof.c)])
+
+
+@pytest.mark.parametrize("x0", [0, 1, -1])
+def test_degenerate_witness_matches_c_oracle(ctx, tmp_path, x0):
+    """SquareChain witnesses from x0 in {0, 1, -1}: every MSM scalar is 0 or 1, so one bucket
+    receives all n entries of its MSM (cut into n / 32 slices: the heavy-bucket path of the
+    fixup) or none at all; every entry point must still equal the C oracle."""
+    import shutil
+    import oracle_c
+    import bn254_ref as o
+    src = str(tmp_path / "sq")
+    ctx.synth_square_chain(12, 99, src)
+    dst = tmp_path / "deg"
+    shutil.copytree(src, dst)
+    n = 1 << 12
+    xs = [x0 % o.P_FR]
+    for _ in range(n):
+        xs.append(xs[-1] * xs[-1] % o.P_FR)  # x_0 .. x_N
+    z = [1, xs[n]] + xs[:n]
+    mont = [v * (1 << 256) % o.P_FR for v in z]
+    bendg.ints_to_wire(mont).astype("<u4").tofile(str(dst / "witness.bin"))
+    want, _ = oracle_c.prove_dir(str(dst))
+    proof, _ = ctx.prove_dir(str(dst))
+    assert np.array_equal(proof_words(proof), want)
+    files = bendg.HostFiles(str(dst))
+    key = ctx.pk_upload(files)
+    for _ in range(2):
+        proof, _ = key.prove(files.words("witness"), files.words("rs"))
+        assert np.array_equal(proof_words(proof), want)
+    key.release()
