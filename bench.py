@@ -38,9 +38,13 @@ METRIC = "SquareChain 2^18 ms/proof"
 UNIT = "ms/proof"
 # the reference's own GPU path (Bend 2 CUDA, RTX 5090) at K=18, T total
 REF_GPU_K18_MS = 56083.0
-FQ_MUL_IMAD = 264      # yardstick: 32-bit multiply-adds per 8x32-bit CIOS Fq product
-MADD_FQ_MULS = 11      # yardstick: Fq products per G1 mixed add (madd-2007-bl, 7M + 4S)
-MADD_G2_FQ_MULS = 29   # yardstick: Fq products per G2 mixed add (7*3 + 4*2 Karatsuba)
+# 32-bit multiply-adds the accumulation kernel executes per mixed addition (madd-2008-s):
+#   CIOS Fq product 8 rows x 33 = 264; 512-bit product 8 x 16 = 128; Montgomery reduction
+#   8 x 17 = 136.  G1: 8 CIOS products + Y3 = u v - w z as two 512-bit products and one
+#   reduction (392) = 2504.  G2: 6 Fq2 products at 3 x 128 + 2 x 136 = 656, 2 Fq2 squares at
+#   2 x 264, Y3 as six 512-bit products and two reductions (1040) = 6032.
+MADD_G1_IMAD = 8 * 264 + 2 * 128 + 136
+MADD_G2_IMAD = 6 * (3 * 128 + 2 * 136) + 2 * 2 * 264 + 6 * 128 + 2 * 136
 KERNEL_FAMILIES = ["msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_fixup_g1", "msm_fixup_g2", "msm_reduce_g1",
                    "msm_reduce_g2", "msm_digits", "msm_scatter", "ntt_pass"]
 
@@ -231,8 +235,8 @@ def run_ours(args, dist: Dist):
     g1_sizes = [na, nb, nh, nl]
     entries_g1 = sum(n * window_counts(L, n)[1] for n in g1_sizes)
     entries_g2 = nb * window_counts(L, nb)[1]
-    work = {"msm_bucket_acc_g1": entries_g1 * MADD_FQ_MULS * FQ_MUL_IMAD,
-            "msm_bucket_acc_g2": entries_g2 * MADD_G2_FQ_MULS * FQ_MUL_IMAD}
+    work = {"msm_bucket_acc_g1": entries_g1 * MADD_G1_IMAD,
+            "msm_bucket_acc_g2": entries_g2 * MADD_G2_IMAD}
     roof = None
     if dom in work:
         nl_, tms = stats[dom]
@@ -248,7 +252,7 @@ def run_ours(args, dist: Dist):
                 "unit": "Gimad/s", "frac": round(achieved / (imad_peak / 1e9), 4), "traffic": traffic,
                 "work_per_launch": per_launch_work, "avg_launch_ms": round(avg_ms, 4),
                 "peak_source": "bg_probe_imad on this GPU (32-bit mad.lo/mad.hi chains)",
-                "work_model": "entries x %d Fq-mul (G2: %d) x %d IMAD" % (MADD_FQ_MULS, MADD_G2_FQ_MULS, FQ_MUL_IMAD)}
+                "work_model": "entries x %d IMAD per G1 mixed add (G2: %d)" % (MADD_G1_IMAD, MADD_G2_IMAD)}
     kernel_ms = {f: {"launches": v[0], "ms_per_proof": round(v[1] / args.steps, 3)} for f, v in stats.items()}
 
     # e2e: all .bin files from pinned host memory through bg_prove_host, every step
@@ -498,8 +502,10 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
     rng = np.random.default_rng(args.seed)
 
     def scalars(n):
+        # uniform below 0x30644e72 * 2^224 < r (all but 2^-33 of [0, r)): every window of the
+        # digit expansion, the top one included, sees the spread of a real witness
         w = rng.integers(0, 1 << 32, size=(n, 8), dtype=np.uint64).astype(np.uint32)
-        w[:, 7] &= 0x0fffffff  # < 2^252 < r
+        w[:, 7] = rng.integers(0, 0x30644e72, size=n, dtype=np.uint64).astype(np.uint32)
         return torch.from_numpy(w.view(np.int32)).to(dev)
 
     def packed(name, count_words16):
@@ -542,7 +548,7 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
     launches, tms = ctx.kernel_stats("msm_bucket_acc_g1")
     ctx.profile(False)
     c, W = window_counts(L, n1)
-    work = n1 * W * MADD_FQ_MULS * FQ_MUL_IMAD
+    work = n1 * W * MADD_G1_IMAD
     avg = tms / max(1, launches)
     achieved = work / (avg * 1e-3) / 1e9
     traffic = None
@@ -554,7 +560,7 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
                        "unit": "Gimad/s", "frac": round(achieved / (imad_peak / 1e9), 4), "traffic": traffic,
                        "work_per_launch": work, "avg_launch_ms": round(avg, 4), "launches": launches,
                        "peak_source": "bg_probe_imad on this GPU (32-bit mad.lo/mad.hi chains)",
-                       "work_model": "n W entries x %d Fq-mul x %d IMAD (c=%d, W=%d)" % (MADD_FQ_MULS, FQ_MUL_IMAD, c, W)}
+                       "work_model": "n W entries x %d IMAD per mixed add (c=%d, W=%d)" % (MADD_G1_IMAD, c, W)}
     if only_g1:
         return res
     n2 = 1 << 18

@@ -36,6 +36,7 @@ EXPORTS = (
     "bg_repack_to_wire_dev", "bg_synth_square_chain", "bg_msm_window_bits", "bg_ctx_profile",
     "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch", "bg_prove_footprint",
     "bg_server_create", "bg_server_submit", "bg_server_wait", "bg_server_reserved_bytes", "bg_server_destroy",
+    "bg_ctx_timeline",
 )
 
 
@@ -103,6 +104,7 @@ def lib():
         "bg_synth_square_chain": (i32, [vp, u32, u64, ctypes.c_char_p]),
         "bg_msm_window_bits": (i32, [sz]),
         "bg_ctx_profile": (i32, [vp, i32]),
+        "bg_ctx_timeline": (i32, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "bg_ctx_kernel_stats": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
         "bg_probe_imad": (i32, [vp, i32, u32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "bg_msm_g1_noalloc": (i32, [vp, vp, sz, vp, vp]),
@@ -191,6 +193,20 @@ class Context:
 
     def profile(self, enable: bool):
         self._check(self._L.bg_ctx_profile(self.h, 1 if enable else 0), "bg_ctx_profile")
+
+    def timeline(self, enable: bool):
+        """enable=True starts recording launch spans; enable=False stops and returns
+        [(family, start_ms, end_ms)] in issue order"""
+        if enable:
+            self._check(self._L.bg_ctx_timeline(self.h, 1, None, 0), "bg_ctx_timeline")
+            return []
+        buf = ctypes.create_string_buffer(1 << 22)
+        self._check(self._L.bg_ctx_timeline(self.h, 0, buf, len(buf)), "bg_ctx_timeline")
+        out = []
+        for ln in buf.value.decode().splitlines():
+            name, a, b = ln.split()
+            out.append((name, float(a), float(b)))
+        return out
 
     def kernel_stats(self, name: str):
         n, ms = ctypes.c_uint64(), ctypes.c_double()

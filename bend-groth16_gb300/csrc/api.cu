@@ -183,6 +183,11 @@ void ctx_release(Ctx& c) {
   c.ev_fork = nullptr;
   for (auto& kv : c.events) cudaEventDestroy(kv.second);
   c.events.clear();
+  for (const Ctx::Span& sp : c.spans) {
+    cudaEventDestroy(sp.a);
+    cudaEventDestroy(sp.b);
+  }
+  c.spans.clear();
   c.ws.clear();
   if (c.stream) cudaStreamDestroy(c.stream);
   c.stream = nullptr;
@@ -574,6 +579,37 @@ int bg_ctx_profile(bg_ctx* ctx, int enable) {
       }
     ctx->c.ktimes.clear();
     ctx->c.profile = enable != 0;
+  });
+}
+
+int bg_ctx_timeline(bg_ctx* ctx, int enable, char* buf, size_t cap) {
+  if (!ctx || (!enable && (!buf || cap == 0))) return BG_E_ARG;
+  return guard(ctx, [&] {
+    Ctx& c = ctx->c;
+    cudaSetDevice(c.device);
+    for (int i = 0; i < kStreams; i++) BG_CUDA(cudaStreamSynchronize(c.side[i]));
+    BG_CUDA(cudaStreamSynchronize(c.stream));
+    std::string text;
+    if (!enable && !c.spans.empty()) {
+      char line[160];
+      for (const Ctx::Span& sp : c.spans) {
+        float t0 = 0, t1 = 0;
+        BG_CUDA(cudaEventElapsedTime(&t0, c.spans[0].a, sp.a));
+        BG_CUDA(cudaEventElapsedTime(&t1, c.spans[0].a, sp.b));
+        snprintf(line, sizeof line, "%s %.4f %.4f\n", sp.name.c_str(), t0, t1);
+        text += line;
+      }
+    }
+    for (const Ctx::Span& sp : c.spans) {
+      cudaEventDestroy(sp.a);
+      cudaEventDestroy(sp.b);
+    }
+    c.spans.clear();
+    c.timeline = enable != 0;
+    if (!enable) {
+      require(text.size() < cap, "bg_ctx_timeline: buffer too small for the recorded spans");
+      memcpy(buf, text.c_str(), text.size() + 1);
+    }
   });
 }
 

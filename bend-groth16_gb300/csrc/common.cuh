@@ -117,7 +117,8 @@ class PinnedCache {
   std::map<std::string, PinnedBuf> bufs_;
 };
 
-constexpr int kStreams = 6;
+constexpr int kStreams = 7;
+constexpr int kSortStream = 6;  // side stream of a proof's bucket sorts
 
 // NTT tables for one domain size 2^L (device pointers into the context workspace)
 struct NttTables {
@@ -156,6 +157,13 @@ struct Ctx {
     double total_ms = 0;
   };
   std::map<std::string, KernelTimes> ktimes;
+  // optional launch timeline: (family, start, end) events of every timed launch, in order
+  bool timeline = false;
+  struct Span {
+    std::string name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Span> spans;
   // named events for cross-stream ordering, created on first use
   std::map<std::string, cudaEvent_t> events;
   cudaEvent_t event(const std::string& name) {
@@ -172,6 +180,13 @@ struct Ctx {
 class KernelTimer {
  public:
   KernelTimer(Ctx& c, const char* name, cudaStream_t st) : c_(c), st_(st) {
+    if (c.timeline) {
+      span_ = true;
+      name_ = name;
+      cudaEventCreate(&ta_);
+      cudaEventCreate(&tb_);
+      cudaEventRecord(ta_, st);
+    }
     if (!c.profile) return;
     kt_ = &c.ktimes[name];
     cudaEventCreate(&a_);
@@ -179,6 +194,10 @@ class KernelTimer {
     cudaEventRecord(a_, st);
   }
   ~KernelTimer() {
+    if (span_) {
+      cudaEventRecord(tb_, st_);
+      c_.spans.push_back({name_, ta_, tb_});
+    }
     if (!kt_) return;
     cudaEventRecord(b_, st_);
     kt_->pending.push_back({a_, b_});
@@ -190,6 +209,9 @@ class KernelTimer {
   cudaStream_t st_;
   Ctx::KernelTimes* kt_ = nullptr;
   cudaEvent_t a_ = nullptr, b_ = nullptr;
+  bool span_ = false;
+  const char* name_ = nullptr;
+  cudaEvent_t ta_ = nullptr, tb_ = nullptr;
 };
 
 // device status flag bits

@@ -223,8 +223,11 @@ BG_DEV Fp<P> mul(const Fp<P>& a, const Fp<P>& b) {
 }
 #undef BG_CIOS_ROW
 
+// squaring product (28 off-diagonal limb products doubled, then one reduction; fp_wide.cuh)
 template <class P>
-BG_DEV Fp<P> sqr(const Fp<P>& a) { return mul(a, a); }
+BG_DEV Fp<P> sqr_wide(const Fp<P>& a);
+template <class P>
+BG_DEV Fp<P> sqr(const Fp<P>& a) { return sqr_wide(a); }
 
 // Out-of-line product for code-size-critical kernels (the curve formulas): every call site
 // shares one copy of the ~300-instruction CIOS body, so a mixed addition is a few hundred
@@ -320,3 +323,5 @@ BG_DEV void store_fp(uint32_t* dst, const Fp<P>& x) {
 }
 
 }  // namespace bg
+
+#include "fp_wide.cuh"

@@ -12,8 +12,10 @@
 //   2. exclusive scan of the histogram -> bucket offsets
 //   3. k_scatter      (point index | sign << 31) written into bucket order
 //   4. k_bucket_acc   load-balanced slices of K entries per thread: XYZZ accumulator += +-P
-//                     (mixed add); k_bucket_fixup joins buckets cut by slice boundaries
-//   5. k_window_reduce one CTA per window part: running sums over 16 buckets per thread, an
+//                     (mixed add); a bucket cut by slice boundaries leaves pieces, joined
+//                     where the reduction reads it (k_bucket_heavy first joins the rare
+//                     buckets of very many pieces)
+//   5. k_window_reduce one CTA per window part: running sums over M buckets per thread, an
 //                     in-CTA suffix scan and tree sum give sum_b (b+1) B_b for the part
 //   6. host: parts -> window sums -> Horner with c doublings per window -> affine.
 // Window sums and the final point are exact group elements, so the affine result equals the
@@ -23,6 +25,7 @@
 #include "host_ff.hpp"
 #include "msm.h"
 
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -200,16 +203,22 @@ __global__ void __launch_bounds__(128) k_build_table(const uint32_t* __restrict_
 // entries, one per thread, so every thread runs exactly K mixed additions whatever the bucket
 // sizes are (one thread per bucket would idle most lanes of a warp on Poisson-sized buckets).
 // A run of entries that covers a whole bucket is written to that bucket; a run cut by a slice
-// boundary becomes a partial: entry 2t of the partial list if the run started in an earlier
-// slice, entry 2t+1 if the bucket starts in slice t and continues into a later one.  owner[t]
-// names that bucket (0xffffffff when slice t ends on a bucket boundary), so a bucket cut into
-// slices t0..t1 has its partials at 2 t0 + 1 and 2 t for t0 < t <= t1 (k_bucket_fixup).
+// boundary becomes a piece: entry 2t of the piece list if the run started in an earlier slice,
+// entry 2t+1 if the bucket starts in slice t and continues into a later one.  So a bucket with
+// entries [o, o') cut into slices t0 = o / K .. t1 = (o' - 1) / K has its pieces at 2 t0 + 1
+// and 2 u for t0 < u <= t1; the window reduction adds them where it reads the bucket
+// (bucket_value), which costs the same additions as a separate join pass without its launch
+// and its mostly idle lanes.  A bucket of more than kPieceLimit + 1 pieces (a scalar value
+// repeated thousands of times) is joined beforehand by k_bucket_heavy: the thread that owns its
+// first piece lists it in heavy[1 + i] (heavy[0] counts, cleared before the accumulation).
+constexpr uint32_t kPieceLimit = 8;
+
 template <class F>
 __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__ points,
                                                     const uint32_t* __restrict__ offsets,
                                                     const uint32_t* __restrict__ sorted, uint32_t nbuckets,
                                                     uint32_t K, uint32_t* __restrict__ buckets,
-                                                    uint32_t* __restrict__ parts, uint32_t* __restrict__ owner) {
+                                                    uint32_t* __restrict__ parts, uint32_t* __restrict__ heavy) {
   constexpr int FW = FieldWords<F>::value;
   constexpr int PW = 4 * FW;
   const uint32_t total = offsets[nbuckets];
@@ -229,7 +238,6 @@ __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__
   // step; a bucket boundary only costs a short divergent flush.
   uint32_t b = lo;
   uint32_t bstart = offsets[b], bend = offsets[b + 1];
-  uint32_t continues = 0xffffffffu;
   XYZZ<F> acc = xyzz_inf<F>();
   for (uint32_t e = beg; e < end; e++) {
     const uint32_t code = sorted[e];
@@ -240,7 +248,7 @@ __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__
       if (bstart < beg || bend > end) {
         const size_t slot = 2 * (size_t)t + (bstart < beg ? 0 : 1);
         store_xyzz(parts + slot * PW, acc);
-        if (bstart >= beg) continues = b;
+        if (bstart >= beg && (bend - 1) / K - t > kPieceLimit) heavy[1 + atomicAdd(heavy, 1u)] = b;
       } else {
         store_xyzz(buckets + (size_t)b * PW, acc);
       }
@@ -254,52 +262,22 @@ __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__
       }
     }
   }
-  owner[t] = continues;
 }
 
-// Buckets cut by slice boundaries.  Thread t serves the bucket that starts in slice t and
-// continues (owner[t]); its partials are entry 2t + 1 and entries 2u for t < u <= t1, t1 the
-// slice of the bucket's last entry.  Up to kFixupChain further partials are added here, one
-// chain per cut bucket (most buckets span two or three slices); a bucket spanning more slices
-// is listed in heavy[1 + i] (heavy[0] counts them) for k_bucket_heavy.
-constexpr uint32_t kFixupChain = 8;
-
-template <class F>
-__global__ void __launch_bounds__(128) k_bucket_fixup(const uint32_t* __restrict__ offsets, uint32_t nbuckets,
-                                                      const uint32_t* __restrict__ parts,
-                                                      const uint32_t* __restrict__ owner, uint32_t K,
-                                                      uint32_t* __restrict__ buckets, uint32_t* __restrict__ heavy) {
-  constexpr int PW = 4 * FieldWords<F>::value;
-  const uint32_t total = offsets[nbuckets];
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if ((uint64_t)t * K >= total) return;
-  const uint32_t b = owner[t];
-  if (b == 0xffffffffu) return;
-  const uint32_t t1 = (offsets[b + 1] - 1) / K;
-  if (t1 - t > kFixupChain) {
-    heavy[1 + atomicAdd(heavy, 1u)] = t;
-    return;
-  }
-  XYZZ<F> acc = load_xyzz<F>(parts + (2 * (size_t)t + 1) * PW);
-  for (uint32_t u = t + 1; u <= t1; u++) acc = xyzz_add(acc, load_xyzz<F>(parts + 2 * (size_t)u * PW));
-  store_xyzz(buckets + (size_t)b * PW, acc);
-}
-
-// Heavy buckets (more than kFixupChain + 1 partials): one CTA per bucket, a strided sum per
-// thread and a tree over the CTA.  The grid is fixed; CTAs loop over however many the fixup
-// listed (none for uniformly spread scalars).
+// Heavy buckets: one CTA per bucket, a strided sum of its pieces per thread and a tree over the
+// CTA; the sum goes to the bucket.  The grid is fixed; CTAs loop over however many the
+// accumulation listed (none for uniformly spread scalars).
 template <class F>
 __global__ void __launch_bounds__(128) k_bucket_heavy(const uint32_t* __restrict__ offsets,
-                                                      const uint32_t* __restrict__ parts,
-                                                      const uint32_t* __restrict__ owner, uint32_t K,
+                                                      const uint32_t* __restrict__ parts, uint32_t K,
                                                       const uint32_t* __restrict__ heavy,
                                                       uint32_t* __restrict__ buckets) {
   constexpr int PW = 4 * FieldWords<F>::value;
   extern __shared__ uint32_t sm[];
   const uint32_t nh = heavy[0];
   for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
-    const uint32_t t0 = heavy[1 + h];
-    const uint32_t b = owner[t0];
+    const uint32_t b = heavy[1 + h];
+    const uint32_t t0 = offsets[b] / K;
     const uint32_t np = (offsets[b + 1] - 1) / K - t0 + 1;
     XYZZ<F> acc = xyzz_inf<F>();
     for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
@@ -322,27 +300,29 @@ __global__ void __launch_bounds__(128) k_bucket_heavy(const uint32_t* __restrict
 constexpr uint32_t kHeavyThreads = 128;
 constexpr uint32_t kHeavyGrid = 152;
 
-// empty buckets hold infinity (no run writes them); also clears the heavy-bucket count
+// acc += value of bucket `key` (entries [offsets[key], offsets[key+1])): nothing when empty, the
+// stored bucket when it lies in one slice or is heavy, else its pieces.
 template <class F>
-__global__ void k_bucket_empty(const uint32_t* __restrict__ offsets, uint32_t nbuckets,
-                               uint32_t* __restrict__ buckets, uint32_t* __restrict__ heavy) {
+BG_DEV XYZZ<F> add_bucket(XYZZ<F> acc, const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ buckets,
+                          const uint32_t* __restrict__ parts, uint32_t K, size_t key) {
   constexpr int PW = 4 * FieldWords<F>::value;
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b == 0) heavy[0] = 0;
-  if (b < nbuckets && offsets[b] == offsets[b + 1]) store_xyzz(buckets + (size_t)b * PW, xyzz_inf<F>());
+  const uint32_t o0 = offsets[key], o1 = offsets[key + 1];
+  if (o1 == o0) return acc;
+  const uint32_t t0 = o0 / K, t1 = (o1 - 1) / K;
+  if (t0 == t1 || t1 - t0 > kPieceLimit) return xyzz_add(acc, load_xyzz<F>(buckets + key * PW));
+  acc = xyzz_add(acc, load_xyzz<F>(parts + (2 * (size_t)t0 + 1) * PW));
+  for (uint32_t u = t0 + 1; u <= t1; u++) acc = xyzz_add(acc, load_xyzz<F>(parts + 2 * (size_t)u * PW));
+  return acc;
 }
 
-// entries per accumulation thread (the fixup adds one point per slice boundary, 1/32 of the
-// accumulation's additions)
+// entries per accumulation thread
 template <class F>
 constexpr uint32_t kSlice = 32;
 
-// Scratch of the bucket phase for at most max_entries entries (words): partials, owners and
-// the heavy list.
+// Scratch of the bucket phase for at most max_entries entries (words): pieces and the heavy list.
 struct BucketScratch {
   uint32_t* parts = nullptr;  // 2 x slices XYZZ points
-  uint32_t* owner = nullptr;  // slices
-  uint32_t* heavy = nullptr;  // 1 + slices / kFixupChain + 1
+  uint32_t* heavy = nullptr;  // 1 + slices / kPieceLimit + 1
 };
 template <class F>
 inline size_t bucket_slices(size_t max_entries) {
@@ -354,42 +334,34 @@ BucketScratch bucket_scratch(size_t max_entries, Get get) {
   const size_t s = bucket_slices<F>(max_entries);
   BucketScratch b;
   b.parts = get("parts", 2 * s * PW);
-  b.owner = get("owner", s);
-  b.heavy = get("heavy", s / kFixupChain + 2);
+  b.heavy = get("heavy", s / kPieceLimit + 2);
   return b;
 }
 
-// Accumulation on `st`: buckets of single-slice runs are final, cut buckets leave partials.
+// Accumulation on `st`: buckets of single-slice runs are final, cut buckets leave pieces.
 template <class F>
 void bucket_accumulate(Ctx* prof, cudaStream_t st, const uint32_t* points, const uint32_t* offsets,
                        const uint32_t* sorted, uint32_t nkeys, size_t max_entries, uint32_t* buckets,
                        const BucketScratch& s) {
   constexpr int FW = FieldWords<F>::value;
   const size_t slices = bucket_slices<F>(max_entries);
+  BG_CUDA(cudaMemsetAsync(s.heavy, 0, sizeof(uint32_t), st));
   std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st)
                                        : nullptr);
   k_bucket_acc<F><<<ceil_div(slices, 128), 128, 0, st>>>(points, offsets, sorted, nkeys, kSlice<F>, buckets, s.parts,
-                                                         s.owner);
+                                                         s.heavy);
   BG_CHECK_LAUNCH();
 }
 
-// Empty buckets, cut buckets and heavy buckets on `st`; afterwards buckets[b] holds the sum
-// of bucket b for every b.
+// Heavy buckets on `st` (a pass that exits at once when there are none).
 template <class F>
-void bucket_fixup(Ctx* prof, cudaStream_t st, const uint32_t* offsets, uint32_t nkeys, size_t max_entries,
-                  uint32_t* buckets, const BucketScratch& s) {
+void bucket_heavy(Ctx* prof, cudaStream_t st, const uint32_t* offsets, uint32_t* buckets, const BucketScratch& s) {
   constexpr int FW = FieldWords<F>::value;
   constexpr int PW = 4 * FW;
-  const size_t slices = bucket_slices<F>(max_entries);
-  std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_fixup_g1" : "msm_fixup_g2", st)
+  std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_heavy_g1" : "msm_heavy_g2", st)
                                        : nullptr);
-  k_bucket_empty<F><<<ceil_div(nkeys, 128), 128, 0, st>>>(offsets, nkeys, buckets, s.heavy);
-  BG_CHECK_LAUNCH();
-  k_bucket_fixup<F><<<ceil_div(slices, 128), 128, 0, st>>>(offsets, nkeys, s.parts, s.owner, kSlice<F>, buckets,
-                                                           s.heavy);
-  BG_CHECK_LAUNCH();
   k_bucket_heavy<F><<<kHeavyGrid, kHeavyThreads, kHeavyThreads * PW * sizeof(uint32_t), st>>>(
-      offsets, s.parts, s.owner, kSlice<F>, s.heavy, buckets);
+      offsets, s.parts, kSlice<F>, s.heavy, buckets);
   BG_CHECK_LAUNCH();
 }
 
@@ -399,17 +371,19 @@ void bucket_fixup(Ctx* prof, cudaStream_t st, const uint32_t* offsets, uint32_t 
 //   S_j = sum_{local b} (b+1) B_b = sum_t T_t + M sum_{t>=1} Suf_t,   Suf_t = sum_{t'>=t} R_t'
 // comes from an in-CTA suffix scan of R and a tree sum; the part also reports R_j = Suf_0.
 // The host finishes window w as sum_j S_j + (RT M) sum_j j R_j.
+// Bucket values are read through add_bucket (stored bucket or its pieces).
 template <class F>
-__global__ void k_window_reduce(const uint32_t* __restrict__ buckets, uint32_t nb, uint32_t M, uint32_t J,
+__global__ void k_window_reduce(const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ buckets,
+                                const uint32_t* __restrict__ pieces, uint32_t K, uint32_t nb, uint32_t M, uint32_t J,
                                 uint32_t* __restrict__ out) {
   constexpr int PW = 4 * FieldWords<F>::value;
   extern __shared__ uint32_t sm[];
   const uint32_t RT = blockDim.x;
   const uint32_t w = blockIdx.x / J, j = blockIdx.x % J, t = threadIdx.x;
-  const uint32_t* B = buckets + ((size_t)w * nb + ((size_t)j * RT + t) * M) * PW;
+  const size_t key0 = (size_t)w * nb + ((size_t)j * RT + t) * M;
   XYZZ<F> run = xyzz_inf<F>(), acc = xyzz_inf<F>();
   for (int k = (int)M - 1; k >= 0; k--) {
-    run = xyzz_add(run, load_xyzz<F>(B + (size_t)k * PW));
+    run = add_bucket(run, offsets, buckets, pieces, K, key0 + k);
     acc = xyzz_add(acc, run);
   }
   // inclusive suffix scan of R over the CTA (Hillis-Steele)
@@ -446,21 +420,53 @@ __global__ void k_window_reduce(const uint32_t* __restrict__ buckets, uint32_t n
   }
 }
 
-// Shape of the window reduction: RT threads x M buckets per thread x J parts per window.
-// With one shared bucket set (window tables) the reduction is the only one of its MSM and its
-// dependent chain (2M additions + two log2(RT) trees) is the tail of the MSM, so it runs with
-// M = 4 and more parts (the host adds J parts in microseconds); with a bucket set per window
-// there are already W x J CTAs and M = 16 keeps the host's share small.
+// Shape of the window reduction: RT threads x M buckets per thread x J parts per window, picked
+// by a latency model.  A thread's dependent chain is M (2 + e / K) additions (each bucket
+// costs its pieces, about 1 + e / K for e entries per bucket, plus the running-sum addition),
+// two log2(RT) trees and log2(M) doublings, times the number of waves the sets x J CTAs need
+// at the kernel's occupancy; the host then adds 3 J points per bucket set, at about 1/16 of a
+// device addition's latency each (a single dependent chain is ~20x faster on a CPU core than
+// on one GPU thread).
 struct ReduceShape {
   uint32_t RT, M, J;
 };
-inline ReduceShape reduce_shape(uint32_t nb, int sets) {
-  ReduceShape s;
-  s.RT = nb < 256 ? nb : 256;
-  const uint32_t mmax = sets == 1 ? 4u : 16u;
-  s.M = (nb / s.RT) < mmax ? nb / s.RT : mmax;
-  s.J = nb / (s.RT * s.M);
-  return s;
+template <class F>
+int reduce_blocks_per_sm(uint32_t RT) {
+  static int cache[9] = {};
+  int lrt = 0;
+  while ((1u << lrt) < RT) lrt++;
+  if (!cache[lrt]) {
+    int n = 0;
+    BG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_window_reduce<F>, (int)RT,
+                                                          RT * 4 * FieldWords<F>::value * sizeof(uint32_t)));
+    cache[lrt] = n > 0 ? n : 1;
+  }
+  return cache[lrt];
+}
+template <class F>
+ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, int sm_count) {
+  const double e = (double)entries / ((double)nb * sets);
+  const double per_bucket = 2.0 + e / 32.0;
+  ReduceShape best{nb < 32 ? nb : 32, 1, 1};
+  best.J = nb / best.RT;
+  double best_cost = 1e300;
+  for (uint32_t RT = 32; RT <= 256; RT <<= 1) {
+    for (uint32_t M = 1; M <= 16; M <<= 1) {
+      if ((uint64_t)RT * M > nb) continue;
+      const uint32_t J = nb / (RT * M);
+      int lrt = 0, lm = 0;
+      while ((1u << lrt) < RT) lrt++;
+      while ((1u << lm) < M) lm++;
+      const double slots = (double)sm_count * reduce_blocks_per_sm<F>(RT);
+      const double waves = std::ceil((double)J * sets / slots);
+      const double cost = waves * (M * per_bucket + 2.0 * lrt + lm) + 3.0 * J * sets / 16.0;
+      if (cost < best_cost) {
+        best_cost = cost;
+        best = {RT, M, J};
+      }
+    }
+  }
+  return best;
 }
 
 // ---------------------------------------------------------------- host driver
@@ -484,81 +490,111 @@ struct HostField<Fq2> {
   typedef bgh::Fq2Ops T;
 };
 
-template <class F>
-void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
-                const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce, const MsmTable* table) {
-  constexpr int FW = FieldWords<F>::value;
-  constexpr int PW = 4 * FW;
-  if (n == 0) {
-    plan.W = 0;
-    return;
-  }
+void msm_sort(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_scalars, size_t n, int c,
+              bool shared_set, MsmSort& out) {
+  out = MsmSort();
+  out.n = n;
+  if (n == 0) return;
   if (n >= 0x80000000ull) throw Error(BG_E_ARG, "msm: n must be below 2^31");
-  if (table && table->n != n) throw Error(BG_E_ARG, "msm: window table built for another size");
-  msm_init_kernels();
-  const int c = table ? table->c : (plan.c > 0 ? plan.c : msm_pick_c(n));
+  if (c < 2 || c > 24) throw Error(BG_E_ARG, "msm: window width out of range");
   const int W = 254 / c + 1;
   const uint32_t nb = 1u << (c - 1);
-  const int sets = table ? 1 : W;  // bucket sets
+  const int sets = shared_set ? 1 : W;
   const size_t nkeys = (size_t)sets * nb;
-  const uint32_t key_stride = table ? 0u : nb;
-  const uint32_t idx_stride = table ? (uint32_t)n : 0u;
-  if (table) d_points = table->d;
-  plan.c = c;
-  plan.W = sets;
+  const uint32_t key_stride = shared_set ? 0u : nb;
+  const uint32_t idx_stride = shared_set ? (uint32_t)n : 0u;
   const size_t max_entries = n * (size_t)W;
   if (max_entries >= 0x80000000ull) throw Error(BG_E_ARG, "msm: n x windows must be below 2^31");
+  out.c = c;
+  out.W = W;
+  out.sets = sets;
+  out.nb = nb;
+  out.nkeys = nkeys;
+  out.max_entries = max_entries;
 
   Workspace& ws = ctx.ws;
   uint32_t* counts = ws.get_t<uint32_t>(tag + ".counts", nkeys + 1);
-  uint32_t* offsets = ws.get_t<uint32_t>(tag + ".offsets", nkeys + 1);
   uint32_t* cursor = ws.get_t<uint32_t>(tag + ".cursor", nkeys + 1);
-  uint32_t* sorted = ws.get_t<uint32_t>(tag + ".sorted", max_entries);
-  uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", nkeys * PW);
-  const BucketScratch bs = bucket_scratch<F>(
-      max_entries, [&](const char* name, size_t words) { return ws.get_t<uint32_t>(tag + ".slice_" + name, words); });
-
+  out.offsets = ws.get_t<uint32_t>(tag + ".offsets", nkeys + 1);
+  out.sorted = ws.get_t<uint32_t>(tag + ".sorted", max_entries);
   BG_CUDA(cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
   {
     KernelTimer kt(ctx, "msm_digits", st);
     k_digits_hist<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, key_stride, counts, ctx.d_status);
     BG_CHECK_LAUNCH();
   }
-  exclusive_scan(ws, tag, counts, offsets, nkeys + 1, st, 0);
-  BG_CUDA(cudaMemcpyAsync(cursor, offsets, (nkeys + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+  exclusive_scan(ws, tag, counts, out.offsets, nkeys + 1, st, 0);
+  BG_CUDA(cudaMemcpyAsync(cursor, out.offsets, (nkeys + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
   {
     KernelTimer kt(ctx, "msm_scatter", st);
-    k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, key_stride, idx_stride, cursor, sorted);
+    k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, key_stride, idx_stride, cursor, out.sorted);
     BG_CHECK_LAUNCH();
   }
-  Ctx* prof = ctx.profile ? &ctx : nullptr;
-  bucket_accumulate<F>(prof, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets, bs);
-  plan.entries = max_entries;
+  out.done = ctx.event(tag + ".sorted");
+  BG_CUDA(cudaEventRecord(out.done, st));
+}
+
+template <class F>
+void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points, const MsmSort& so,
+                    MsmPlan& plan, cudaStream_t st_reduce, const MsmTable* table) {
+  constexpr int FW = FieldWords<F>::value;
+  constexpr int PW = 4 * FW;
+  if (so.n == 0) {
+    plan.W = 0;
+    return;
+  }
+  if (table && (table->n != so.n || table->c != so.c || so.sets != 1))
+    throw Error(BG_E_ARG, "msm: window table and bucket order disagree");
+  if (!table && so.sets == 1) throw Error(BG_E_ARG, "msm: a shared bucket set needs a window table");
+  msm_init_kernels();
+  if (table) d_points = table->d;
+  plan.c = so.c;
+  plan.W = so.sets;
+  plan.entries = so.max_entries;
+  Workspace& ws = ctx.ws;
+  uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", so.nkeys * PW);
+  const BucketScratch bs = bucket_scratch<F>(
+      so.max_entries, [&](const char* name, size_t words) { return ws.get_t<uint32_t>(tag + ".slice_" + name, words); });
+  if (so.done) BG_CUDA(cudaStreamWaitEvent(st, so.done, 0));
+  Ctx* prof = (ctx.profile || ctx.timeline) ? &ctx : nullptr;
+  bucket_accumulate<F>(prof, st, d_points, so.offsets, so.sorted, (uint32_t)so.nkeys, so.max_entries, buckets, bs);
 
   cudaStream_t rs = st;
   if (st_reduce && st_reduce != st) {
-    // the latency-bound fixup and reduction run on their own stream and overlap whatever `st`
-    // does next (the next MSM's accumulation)
+    // the latency-bound heavy-bucket pass and reduction run on their own stream and overlap
+    // whatever `st` does next (the next MSM's accumulation)
     cudaEvent_t ev = ctx.event(tag + ".acc_done");
     BG_CUDA(cudaEventRecord(ev, st));
     BG_CUDA(cudaStreamWaitEvent(st_reduce, ev, 0));
     rs = st_reduce;
   }
-  bucket_fixup<F>(prof, rs, offsets, (uint32_t)nkeys, max_entries, buckets, bs);
+  bucket_heavy<F>(prof, rs, so.offsets, buckets, bs);
 
-  const ReduceShape rsh = reduce_shape(nb, sets);
+  const ReduceShape rsh = reduce_shape<F>(so.nb, so.sets, so.max_entries, ctx.sm_count);
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
-  uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)sets * J * 2 * PW);
+  uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)so.sets * J * 2 * PW);
   {
     KernelTimer kt(ctx, FW == 8 ? "msm_reduce_g1" : "msm_reduce_g2", rs);
-    k_window_reduce<F><<<sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(buckets, nb, M, J, parts);
+    k_window_reduce<F><<<so.sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(so.offsets, buckets, bs.parts,
+                                                                             kSlice<F>, so.nb, M, J, parts);
     BG_CHECK_LAUNCH();
   }
   plan.fetch_stream = rs;
   plan.J = J;
   plan.part_span = RT * M;
   plan.d_window_sums = parts;
-  plan.host_window_sums = ctx.host_cache.get_t<uint32_t>(tag + ".window_sums", (size_t)sets * J * 2 * PW);
+  plan.host_window_sums = ctx.host_cache.get_t<uint32_t>(tag + ".window_sums", (size_t)so.sets * J * 2 * PW);
+}
+
+template <class F>
+void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
+                const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce, const MsmTable* table) {
+  if (table && table->n != n) throw Error(BG_E_ARG, "msm: window table built for another size");
+  const int c = table ? table->c : (plan.c > 0 ? plan.c : msm_pick_c(n));
+  MsmSort so;
+  msm_sort(ctx, st, tag, d_scalars, n, c, table != nullptr, so);
+  so.done = nullptr;  // same stream: already ordered
+  msm_accumulate<F>(ctx, st, tag, d_points, so, plan, st_reduce, table);
 }
 
 int msm_pick_c_table(size_t n) {
@@ -636,6 +672,10 @@ void msm_init_kernels() {
 
 template void msm_launch<Fq>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const uint32_t*, size_t,
                              MsmPlan&, cudaStream_t, const MsmTable*);
+template void msm_accumulate<Fq>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const MsmSort&, MsmPlan&,
+                                 cudaStream_t, const MsmTable*);
+template void msm_accumulate<Fq2>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const MsmSort&, MsmPlan&,
+                                  cudaStream_t, const MsmTable*);
 template void msm_launch<Fq2>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const uint32_t*, size_t,
                               MsmPlan&, cudaStream_t, const MsmTable*);
 template void msm_fetch<Fq>(cudaStream_t, MsmPlan&);
@@ -707,7 +747,11 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   const uint32_t nb = 1u << (c - 1);
   const size_t nkeys = (size_t)W * nb;
   const size_t max_entries = n * (size_t)W;
-  const ReduceShape rsh = reduce_shape(nb, W);
+  int dev = 0, sms = 0;
+  BG_CUDA(cudaGetDevice(&dev));
+  BG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  msm_init_kernels();
+  const ReduceShape rsh = reduce_shape<Fq>(nb, W, max_entries, sms);
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
   const unsigned tiles = ceil_div(nkeys + 1, kScanTile);
 
@@ -751,8 +795,9 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   k_scatter<<<ceil_div(n, 256), 256, 0, st>>>(d_scalars, n, c, W, nb, 0, cursor, sorted);
   BG_CHECK_LAUNCH();
   bucket_accumulate<Fq>(nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets, bs);
-  bucket_fixup<Fq>(nullptr, st, offsets, (uint32_t)nkeys, max_entries, buckets, bs);
-  k_window_reduce<Fq><<<W * J, RT, RT * PW * sizeof(uint32_t), st>>>(buckets, nb, M, J, parts);
+  bucket_heavy<Fq>(nullptr, st, offsets, buckets, bs);
+  k_window_reduce<Fq><<<W * J, RT, RT * PW * sizeof(uint32_t), st>>>(offsets, buckets, bs.parts, kSlice<Fq>, nb, M, J,
+                                                                     parts);
   BG_CHECK_LAUNCH();
   BG_CUDA(cudaMemcpyAsync(g_noalloc_host_parts, parts, host_words * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   BG_CUDA(cudaMemcpyAsync(&g_noalloc_host_status, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));

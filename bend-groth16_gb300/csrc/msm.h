@@ -28,6 +28,19 @@ struct MsmTable {
   int c = 0, W = 0;
 };
 
+// Bucket order of one scalar vector for one window layout (c-bit signed digits; one bucket set
+// per window, or one set shared by all windows for window tables).  It depends on the scalars
+// and the layout only, so MSMs over the same scalars and layout share it.
+struct MsmSort {
+  size_t n = 0;
+  int c = 0, W = 0, sets = 0;
+  uint32_t nb = 0;
+  size_t nkeys = 0, max_entries = 0;
+  uint32_t* offsets = nullptr;  // nkeys + 1 bucket offsets into sorted
+  uint32_t* sorted = nullptr;   // entries: point index (+ w n for tables) | sign << 31
+  cudaEvent_t done = nullptr;   // recorded after the scatter (null: ordered by the stream)
+};
+
 int msm_pick_c(size_t n);
 int msm_pick_c_table(size_t n);
 void msm_init_kernels();
@@ -45,6 +58,13 @@ template <class F>
 void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
                 const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce = nullptr,
                 const MsmTable* table = nullptr);
+// The two halves of msm_launch: the sort on `st` (records so.done), and everything after it
+// on `st` (waits for so.done) with the fixup and reduction on `st_reduce`.
+void msm_sort(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_scalars, size_t n, int c,
+              bool shared_set, MsmSort& out);
+template <class F>
+void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points, const MsmSort& so,
+                    MsmPlan& plan, cudaStream_t st_reduce = nullptr, const MsmTable* table = nullptr);
 // Enqueue the copy of the window sums to the host.
 template <class F>
 void msm_fetch(cudaStream_t st, MsmPlan& plan);

@@ -14,6 +14,7 @@
 // s A + r B1, ...) while msm_h is still running, so only msm_h's finish is left at the end.
 #include <chrono>
 #include <cstring>
+#include <memory>
 #include <thread>
 
 #include "common.cuh"
@@ -346,12 +347,14 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   uint32_t* ec = ws.get_t<uint32_t>("prove.ec", d * 8);
   const CsrDev* m[3] = {&pk.ca, &pk.cb, &pk.cc};
   uint32_t* ev[3] = {ea, eb, ec};
+  std::unique_ptr<KernelTimer> kt_evals(new KernelTimer(ctx, "evals", st));
   for (int k = 0; k < 3; k++) {
     k_evals<<<ceil_div(d, 128), 128, 0, st>>>(m[k]->offs, m[k]->cols, m[k]->coeffs, z, (uint32_t)nz, h.nc,
                                               k == 0 ? h.ni : 0, d, ev[k], ctx.d_status);
     BG_CHECK_LAUNCH();
   }
   fr_from_mont(st, z, zc, nz);
+  kt_evals.reset();
   t_evals.stop(st);
 
   // ---- QAP on the main stream; it needs only the evaluation vectors
@@ -359,11 +362,12 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   t_qap.start(st);
   uint32_t* hh = ws.get_t<uint32_t>("prove.h", d * 8);
   uint32_t* hc = ws.get_t<uint32_t>("prove.hc", d * 8);
-  qap_h_run(ctx, st, ea, eb, ec, hh, h.lg);
-  fr_from_mont(st, hh, hc, h.nh);
+  {
+    KernelTimer kt(ctx, "qap", st);
+    qap_h_run(ctx, st, ea, eb, ec, hh, h.lg);
+    fr_from_mont(st, hh, hc, h.nh);
+  }
   t_qap.stop(st);
-  cudaEvent_t ev_qap = ctx.event("prove.qap_done");
-  BG_CUDA(cudaEventRecord(ev_qap, st));
 
   // ---- MSM accumulations back to back on one stream (each one fills the GPU), every window
   // reduction on a stream of its own so it overlaps the next accumulation; msm_h goes last
@@ -384,19 +388,43 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
                        {2, "msm_b2", true, pk.pb2, zc, h.nb, tab(2)},
                        {4, "msm_l", false, pk.pl, zc + 8 * (size_t)h.ni, h.nl, tab(4)},
                        {3, "msm_h", false, pk.ph, hc, h.nh, tab(3)}};
+  // Bucket orders first, on their own stream: a, b1 and b2 take the same scalars (the whole
+  // assignment) and, with equal lengths, the same window layout, so they share one sort; l's
+  // follows; h's is made on the main stream once the QAP is done.  The accumulation stream then
+  // runs the five accumulations back to back, each waiting only for its own sort.
   cudaStream_t acc_st = ctx.side[0];
+  cudaStream_t sort_st = ctx.side[kSortStream];
+  BG_CUDA(cudaStreamWaitEvent(sort_st, ctx.ev_fork, 0));
+  struct SortKey {
+    const uint32_t* sc;
+    size_t n;
+    int c;
+    bool shared;
+  };
+  std::vector<std::pair<SortKey, MsmSort>> sorts;
+  sorts.reserve(5);
+  auto sort_for = [&](const Job& jb, cudaStream_t s) -> const MsmSort& {
+    const SortKey k{jb.sc, jb.n, jb.tab ? jb.tab->c : msm_pick_c(jb.n), jb.tab != nullptr};
+    for (auto& e : sorts)
+      if (e.first.sc == k.sc && e.first.n == k.n && e.first.c == k.c && e.first.shared == k.shared) return e.second;
+    sorts.emplace_back(k, MsmSort());
+    msm_sort(ctx, s, std::string(jb.tag) + ".sort", jb.sc, jb.n, k.c, k.shared, sorts.back().second);
+    return sorts.back().second;
+  };
+  const MsmSort* so[5];
+  for (int j = 0; j < 4; j++) so[j] = &sort_for(jobs[j], sort_st);
+  so[4] = &sort_for(jobs[4], st);  // st: after the QAP
   BG_CUDA(cudaStreamWaitEvent(acc_st, ctx.ev_fork, 0));
   for (int j = 0; j < 5; j++) {
     const Job& jb = jobs[j];
     cudaStream_t red = ctx.side[1 + j];
-    if (jb.idx == 3) BG_CUDA(cudaStreamWaitEvent(acc_st, ev_qap, 0));
     MsmPlan& p = plan[jb.idx];
     t_msm[jb.idx].start(acc_st);
     if (jb.g2) {
-      msm_launch<Fq2>(ctx, acc_st, jb.tag, jb.pts, jb.sc, jb.n, p, red, jb.tab);
+      msm_accumulate<Fq2>(ctx, acc_st, jb.tag, jb.pts, *so[j], p, red, jb.tab);
       msm_fetch<Fq2>(acc_st, p);
     } else {
-      msm_launch<Fq>(ctx, acc_st, jb.tag, jb.pts, jb.sc, jb.n, p, red, jb.tab);
+      msm_accumulate<Fq>(ctx, acc_st, jb.tag, jb.pts, *so[j], p, red, jb.tab);
       msm_fetch<Fq>(acc_st, p);
     }
     t_msm[jb.idx].stop(red);
@@ -473,9 +501,9 @@ static size_t msm_footprint(size_t n, bool g2) {
   const size_t PW = g2 ? 64 : 32, K = 32;
   const size_t entries = n * W, threads = (entries + K - 1) / K;
   const size_t RT = nb < 256 ? nb : 256, M = (nb / RT) < 16 ? nb / RT : 16, J = nb / (RT * M);
-  // counters, offsets, cursors, entry list, buckets, slice partials + owners + heavy list,
-  // window parts, scan sums
-  const size_t words = 3 * (nkeys + 1) + entries + nkeys * PW + 2 * threads * PW + threads + threads / 8 + 2 +
+  // counters, offsets, cursors, entry list, buckets, slice pieces + heavy list, window parts,
+  // scan sums
+  const size_t words = 3 * (nkeys + 1) + entries + nkeys * PW + 2 * threads * PW + threads / 8 + 2 +
                        W * J * 2 * PW + 2 * ((nkeys + 1) / 2048 + 1);
   return words * 4;
 }

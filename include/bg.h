@@ -202,6 +202,11 @@ int bg_ctx_profile(bg_ctx* ctx, int enable);
  * "msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_reduce_g1", "msm_reduce_g2", "msm_digits",
  * "msm_scatter", "ntt_pass".  Unknown names report zero launches. */
 int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms);
+/* Launch timeline: enable = 1 clears and starts recording the start and end of every timed
+ * launch (the families above plus the proof phases); enable = 0 stops and writes one line
+ * "family start_ms end_ms" per launch, in issue order, times relative to the first recorded
+ * start, into buf (NUL-terminated; BG_E_ARG when cap is too small). */
+int bg_ctx_timeline(bg_ctx* ctx, int enable, char* buf, size_t cap);
 /* Integer multiply-add throughput probe: which = 0 raw 32-bit mad.lo/mad.hi chains (50/50),
  * 1 Fq Montgomery products, 2 mad.lo only, 3 mad.hi only, 4 mad.wide.u32 only.  Returns the
  * operations executed (instructions, or Fq products for 1) and the kernel time in ms. */
