@@ -38,13 +38,14 @@ METRIC = "SquareChain 2^18 ms/proof"
 UNIT = "ms/proof"
 # the reference's own GPU path (Bend 2 CUDA, RTX 5090) at K=18, T total
 REF_GPU_K18_MS = 56083.0
-# 32-bit multiply-adds the accumulation kernel executes per mixed addition (madd-2008-s):
-#   CIOS Fq product 8 rows x 33 = 264; 512-bit product 8 x 16 = 128; Montgomery reduction
-#   8 x 17 = 136.  G1: 8 CIOS products + Y3 = u v - w z as two 512-bit products and one
-#   reduction (392) = 2504.  G2: 6 Fq2 products at 3 x 128 + 2 x 136 = 656, 2 Fq2 squares at
-#   2 x 264, Y3 as six 512-bit products and two reductions (1040) = 6032.
-MADD_G1_IMAD = 8 * 264 + 2 * 128 + 136
-MADD_G2_IMAD = 6 * (3 * 128 + 2 * 136) + 2 * 2 * 264 + 6 * 128 + 2 * 136
+# 32-bit multiply-adds (mad.lo + mad.hi) the accumulation kernel executes per mixed addition
+# (madd-2008-s), from the products of fp_wide.cuh: a 512-bit Karatsuba product 3 x 32 = 96,
+# a 512-bit square 72, a Montgomery reduction 8 x 17 = 136.  Fq product 232, square 208,
+# u v - w z 2 x 96 + 136 = 328.  G1: 6 products + 2 squares + Y3 = 2136.  G2 (Fq2 product 3 x 96
+# + 2 x 136 = 560, square = 2 Fq products, u v - w z 6 x 96 + 2 x 136 = 848): 6 x 560 +
+# 2 x 464 + 848 = 5136.
+MADD_G1_IMAD = 6 * (96 + 136) + 2 * (72 + 136) + (2 * 96 + 136)
+MADD_G2_IMAD = 6 * (3 * 96 + 2 * 136) + 2 * 2 * (96 + 136) + (6 * 96 + 2 * 136)
 KERNEL_FAMILIES = ["msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_fixup_g1", "msm_fixup_g2", "msm_reduce_g1",
                    "msm_reduce_g2", "msm_digits", "msm_scatter", "ntt_pass"]
 
@@ -120,6 +121,11 @@ def ensure_instance(args, dist: Dist, generator) -> str:
 
 def window_counts(L, n):
     c = L.bg_msm_window_bits(n)
+    return c, 254 // c + 1
+
+
+def table_window_counts(L, n):
+    c = L.bg_msm_table_window_bits(n)
     return c, 254 // c + 1
 
 
@@ -233,8 +239,9 @@ def run_ours(args, dist: Dist):
     ctx.profile(False)
     dom = "msm_bucket_acc_g1"
     g1_sizes = [na, nb, nh, nl]
-    entries_g1 = sum(n * window_counts(L, n)[1] for n in g1_sizes)
-    entries_g2 = nb * window_counts(L, nb)[1]
+    # the timed proofs run against the resident key: window tables, W = floor(254 / c_table) + 1
+    entries_g1 = sum(n * table_window_counts(L, n)[1] for n in g1_sizes)
+    entries_g2 = nb * table_window_counts(L, nb)[1]
     work = {"msm_bucket_acc_g1": entries_g1 * MADD_G1_IMAD,
             "msm_bucket_acc_g2": entries_g2 * MADD_G2_IMAD}
     roof = None
@@ -261,6 +268,7 @@ def run_ours(args, dist: Dist):
     dist.barrier()
     torch.cuda.synchronize()
     e2e_ms = []
+    xfer0 = ctx.transfer_bytes()
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -271,11 +279,13 @@ def run_ours(args, dist: Dist):
         e1.synchronize()
         e2e_ms.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
+    xfer1 = ctx.transfer_bytes()
     dist.barrier()
     e2e_total = dist.max(sum(e2e_ms))
-    d2h = sum(window_counts(L, n)[1] * 128 for n in g1_sizes) + window_counts(L, nb)[1] * 256 + 5 * 4
+    # bytes the library copied (its own counters: file uploads, MSM window sums, status words)
     e2e = {"value": round(aggregate_ms_per_proof(e2e_total, dist.world, args.steps), 3), "unit": UNIT,
-           "h2d_bytes_per_step": int(files.nbytes()), "d2h_bytes_per_step": int(d2h),
+           "h2d_bytes_per_step": (xfer1[0] - xfer0[0]) // args.steps,
+           "d2h_bytes_per_step": (xfer1[1] - xfer0[1]) // args.steps,
            "api": "bg_prove_host (every .bin file uploaded per proof)"}
 
     prims = None if args.no_primitives else primitives(ctx, files, nh, nb, args, ext, flush, imad_peak)
@@ -294,7 +304,8 @@ def run_ours(args, dist: Dist):
                    "log2_constraints": args.log2n, "domain_log2": lg, "n_a": na, "n_b": nb, "n_h": nh, "n_l": nl,
                    "seed": args.seed, "parallelism": "replicas" if dist.world > 1 else "single GPU",
                    "l2": "flushed (512 MiB write) before every timed step",
-                   "msm_window_bits": {str(n): L.bg_msm_window_bits(n) for n in sorted(set(g1_sizes + [nb]))}},
+                   "msm_window_bits": {str(n): L.bg_msm_table_window_bits(n) for n in sorted(set(g1_sizes + [nb]))},
+                   "msm_layout": "resident key: 2^(c w) window tables, one shared bucket set per MSM"},
         "e2e": e2e, "roofline": roof_iso or roof, "roofline_in_proof": roof, "gpu_launches": int(launches), "clocks": clk,
         "phases_ms_median": {k: round(statistics.median(p[k] for p in phases), 3) for k in phases[0]},
         "kernels": kernel_ms, "fq_mul_rate_gops": round(fqmul_rate / 1e9, 2), "primitives": prims,

@@ -36,7 +36,7 @@ EXPORTS = (
     "bg_repack_to_wire_dev", "bg_synth_square_chain", "bg_msm_window_bits", "bg_ctx_profile",
     "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch", "bg_prove_footprint",
     "bg_server_create", "bg_server_submit", "bg_server_wait", "bg_server_reserved_bytes", "bg_server_destroy",
-    "bg_ctx_timeline",
+    "bg_ctx_timeline", "bg_msm_table_window_bits", "bg_ctx_transfer_bytes",
 )
 
 
@@ -103,8 +103,10 @@ def lib():
         "bg_repack_to_wire_dev": (i32, [vp, vp, vp, sz]),
         "bg_synth_square_chain": (i32, [vp, u32, u64, ctypes.c_char_p]),
         "bg_msm_window_bits": (i32, [sz]),
+        "bg_msm_table_window_bits": (i32, [sz]),
         "bg_ctx_profile": (i32, [vp, i32]),
         "bg_ctx_timeline": (i32, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),
+        "bg_ctx_transfer_bytes": (i32, [vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
         "bg_ctx_kernel_stats": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
         "bg_probe_imad": (i32, [vp, i32, u32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "bg_msm_g1_noalloc": (i32, [vp, vp, sz, vp, vp]),
@@ -193,6 +195,12 @@ class Context:
 
     def profile(self, enable: bool):
         self._check(self._L.bg_ctx_profile(self.h, 1 if enable else 0), "bg_ctx_profile")
+
+    def transfer_bytes(self):
+        """(host-to-device, device-to-host) bytes copied by this context so far"""
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._L.bg_ctx_transfer_bytes(self.h, ctypes.byref(a), ctypes.byref(b)), "bg_ctx_transfer_bytes")
+        return int(a.value), int(b.value)
 
     def timeline(self, enable: bool):
         """enable=True starts recording launch spans; enable=False stops and returns

@@ -72,6 +72,7 @@ uint32_t* stage_in(Ctx& c, const std::string& name, const uint32_t* host16, size
   uint32_t* wire = c.ws.get_t<uint32_t>(name + ".wire", n_elems * 16);
   uint32_t* packed = c.ws.get_t<uint32_t>(name, n_elems * 8);
   BG_CUDA(cudaMemcpyAsync(wire, host16, n_elems * 64, cudaMemcpyHostToDevice, c.stream));
+  c.h2d_bytes += n_elems * 64;
   wire_to_packed(c.stream, wire, packed, n_elems, c.d_status);
   return packed;
 }
@@ -80,6 +81,7 @@ void stage_out(Ctx& c, const std::string& name, const uint32_t* d_packed, uint32
   uint32_t* wire = c.ws.get_t<uint32_t>(name + ".wire_out", n_elems * 16);
   packed_to_wire(c.stream, d_packed, wire, n_elems);
   BG_CUDA(cudaMemcpyAsync(host16, wire, n_elems * 64, cudaMemcpyDeviceToHost, c.stream));
+  c.d2h_bytes += n_elems * 64;
 }
 
 // affine packed result -> Jacobian wire words (x, y, z) with z = 1, infinity = (0, 1, 0)
@@ -115,7 +117,7 @@ void msm_host(Ctx& c, const uint32_t* points16, const uint32_t* scalars16, size_
     const uint32_t* sc = stage_in(c, "api.msm_sc", scalars16, n);
     MsmPlan plan;
     msm_launch<F>(c, c.stream, "api.msm", pts, sc, n, plan);
-    msm_fetch<F>(c.stream, plan);
+    msm_fetch<F>(c, c.stream, plan);
     BG_CUDA(cudaStreamSynchronize(c.stream));
     check_status(c, c.stream);
     msm_finish<F>(plan, aff);
@@ -132,7 +134,7 @@ void msm_dev(Ctx& c, const uint32_t* d_points, const uint32_t* d_scalars, size_t
   }
   MsmPlan plan;
   msm_launch<F>(c, c.stream, "api.msm", d_points, d_scalars, n, plan);
-  msm_fetch<F>(c.stream, plan);
+  msm_fetch<F>(c, c.stream, plan);
   BG_CUDA(cudaStreamSynchronize(c.stream));
   check_status(c, c.stream);
   msm_finish<F>(plan, out_aff32);
@@ -276,6 +278,7 @@ void bg_host_free(void* p) {
 }
 
 int bg_msm_window_bits(size_t n) { return msm_pick_c(n); }
+int bg_msm_table_window_bits(size_t n) { return msm_pick_c_table(n); }
 
 int bg_msm_g1(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, size_t n, uint32_t* out_jac16) {
   if (!ctx || !out_jac16 || (n && (!points16 || !scalars16))) return BG_E_ARG;
@@ -609,6 +612,18 @@ int bg_ctx_timeline(bg_ctx* ctx, int enable, char* buf, size_t cap) {
     if (!enable) {
       require(text.size() < cap, "bg_ctx_timeline: buffer too small for the recorded spans");
       memcpy(buf, text.c_str(), text.size() + 1);
+    }
+  });
+}
+
+int bg_ctx_transfer_bytes(bg_ctx* ctx, uint64_t* h2d, uint64_t* d2h) {
+  if (!ctx || !h2d || !d2h) return BG_E_ARG;
+  return guard(ctx, [&] {
+    *h2d = ctx->c.h2d_bytes;
+    *d2h = ctx->c.d2h_bytes;
+    for (auto& l : ctx->lanes) {
+      *h2d += l->h2d_bytes;
+      *d2h += l->d2h_bytes;
     }
   });
 }

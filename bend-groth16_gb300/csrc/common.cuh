@@ -147,6 +147,7 @@ struct Ctx {
   PinnedCache host_cache;
   std::string last_error;
   uint32_t* d_status = nullptr;           // device-side error flags (see BG_DSTATUS_*)
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host <-> device bytes this context has copied
   std::map<int, NttTables> ntt_tabs;      // per domain size, built on first use
   // optional per-kernel timing: CUDA events recorded around selected launches on their
   // own stream, resolved when the statistics are read

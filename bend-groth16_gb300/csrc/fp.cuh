@@ -229,14 +229,6 @@ BG_DEV Fp<P> sqr_wide(const Fp<P>& a);
 template <class P>
 BG_DEV Fp<P> sqr(const Fp<P>& a) { return sqr_wide(a); }
 
-// Out-of-line product for code-size-critical kernels (the curve formulas): every call site
-// shares one copy of the ~300-instruction CIOS body, so a mixed addition is a few hundred
-// instructions instead of several thousand and its loop stays in the instruction cache.
-template <class P>
-__device__ __noinline__ Fp<P> mul_ool(Fp<P> a, Fp<P> b) {
-  return mul(a, b);
-}
-
 // x * 2^-256: Montgomery -> canonical (multiply by the raw integer 1)
 template <class P>
 BG_DEV Fp<P> from_mont(const Fp<P>& a) {

@@ -2,9 +2,11 @@
 // products ("lazy reduction").  A CIOS product spends half of its 264 multiply-adds on the
 // reduction (8 rows x 17); when a formula needs a +- b c +- d e, computing the two 16-limb
 // products, combining them and reducing once saves one reduction, and the Fq2 Karatsuba product
-// (three Fq products, two reductions instead of three) saves one of every six.  A square
-// computes its 28 off-diagonal limb products once and doubles them (72 multiply-adds instead of
-// 128).  Bounds: every value reduced here is below p R (R = 2^256), so the reduction returns
+// (three Fq products, two reductions instead of three) saves one of every six.  The 16-limb
+// product itself is one level of Karatsuba over 128-bit halves (96 multiply-adds instead of
+// 128), and a square computes its 28 off-diagonal limb products once and doubles them (72).
+// The high half of a 32-bit product issues at half the rate of the low half on this GPU, so
+// these counts are what bounds the MSM accumulation.  Bounds: every value reduced here is below p R (R = 2^256), so the reduction returns
 // a value below 2p that one conditional subtraction brings below p; combinations add 2 p^2
 // before subtracting, which keeps them non-negative and below 4 p^2 < p R (4p < 2^256 for the
 // BN254 base field).
@@ -19,162 +21,218 @@ struct Wide {
   uint32_t v[16];
 };
 
-// t = a b (a, b below 2^256)
+// t = a b by one level of Karatsuba on 128-bit halves: a0 b0, a1 b1 and (a0 + a1)(b0 + b1)
+// (three 4 x 4 limb products, 48 multiply-add pairs instead of 64); the half sums carry one
+// bit each, added back as shifted copies of the other sum.
 BG_DEV void wide_mul(Wide& t, const uint32_t* a, const uint32_t* b) {
+  uint32_t p0[8], p2[8], p1[9], sa[4], sb[4], ca, cb;
 #pragma unroll
-  for (int i = 0; i < 16; i++) t.v[i] = 0;
-  asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
-      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
-      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
-      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
-      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
-      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
-      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
-      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
-      "addc.u32       %8, %8, 0;\n\t"
-      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"
-      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"
-      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"
-      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"
-      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"
-      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"
-      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"
-      "madc.hi.u32    %8, %16, %17, %8;"
-      : "+r"(t.v[0]), "+r"(t.v[1]), "+r"(t.v[2]), "+r"(t.v[3]), "+r"(t.v[4]), "+r"(t.v[5]), "+r"(t.v[6]), "+r"(t.v[7]), "+r"(t.v[8])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[0]));
-  asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
-      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
-      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
-      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
-      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
-      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
-      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
-      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
-      "addc.u32       %8, %8, 0;\n\t"
-      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"
-      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"
-      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"
-      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"
-      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"
-      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"
-      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"
-      "madc.hi.u32    %8, %16, %17, %8;"
-      : "+r"(t.v[1]), "+r"(t.v[2]), "+r"(t.v[3]), "+r"(t.v[4]), "+r"(t.v[5]), "+r"(t.v[6]), "+r"(t.v[7]), "+r"(t.v[8]), "+r"(t.v[9])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[1]));
-  asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
-      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
-      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
-      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
-      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
-      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
-      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
-      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
-      "addc.u32       %8, %8, 0;\n\t"
-      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"
-      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"
-      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"
-      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"
-      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"
-      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"
-      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"
-      "madc.hi.u32    %8, %16, %17, %8;"
-      : "+r"(t.v[2]), "+r"(t.v[3]), "+r"(t.v[4]), "+r"(t.v[5]), "+r"(t.v[6]), "+r"(t.v[7]), "+r"(t.v[8]), "+r"(t.v[9]), "+r"(t.v[10])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[2]));
-  asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
-      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
-      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
-      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
-      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
-      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
-      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
-      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
-      "addc.u32       %8, %8, 0;\n\t"
-      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"
-      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"
-      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"
-      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"
-      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"
-      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"
-      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"
-      "madc.hi.u32    %8, %16, %17, %8;"
-      : "+r"(t.v[3]), "+r"(t.v[4]), "+r"(t.v[5]), "+r"(t.v[6]), "+r"(t.v[7]), "+r"(t.v[8]), "+r"(t.v[9]), "+r"(t.v[10]), "+r"(t.v[11])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[3]));
-  asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
-      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
-      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
-      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
-      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
-      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
-      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
-      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
-      "addc.u32       %8, %8, 0;\n\t"
-      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"
-      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"
-      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"
-      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"
-      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"
-      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"
-      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"
-      "madc.hi.u32    %8, %16, %17, %8;"
-      : "+r"(t.v[4]), "+r"(t.v[5]), "+r"(t.v[6]), "+r"(t.v[7]), "+r"(t.v[8]), "+r"(t.v[9]), "+r"(t.v[10]), "+r"(t.v[11]), "+r"(t.v[12])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[4]));
-  asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
-      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
-      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
-      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
-      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
-      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
-      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
-      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
-      "addc.u32       %8, %8, 0;\n\t"
-      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"
-      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"
-      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"
-      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"
-      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"
-      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"
-      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"
-      "madc.hi.u32    %8, %16, %17, %8;"
-      : "+r"(t.v[5]), "+r"(t.v[6]), "+r"(t.v[7]), "+r"(t.v[8]), "+r"(t.v[9]), "+r"(t.v[10]), "+r"(t.v[11]), "+r"(t.v[12]), "+r"(t.v[13])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[5]));
-  asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
-      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
-      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
-      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
-      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
-      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
-      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
-      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
-      "addc.u32       %8, %8, 0;\n\t"
-      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"
-      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"
-      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"
-      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"
-      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"
-      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"
-      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"
-      "madc.hi.u32    %8, %16, %17, %8;"
-      : "+r"(t.v[6]), "+r"(t.v[7]), "+r"(t.v[8]), "+r"(t.v[9]), "+r"(t.v[10]), "+r"(t.v[11]), "+r"(t.v[12]), "+r"(t.v[13]), "+r"(t.v[14])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[6]));
-  asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
-      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
-      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
-      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
-      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
-      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
-      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
-      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
-      "addc.u32       %8, %8, 0;\n\t"
-      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"
-      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"
-      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"
-      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"
-      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"
-      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"
-      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"
-      "madc.hi.u32    %8, %16, %17, %8;"
-      : "+r"(t.v[7]), "+r"(t.v[8]), "+r"(t.v[9]), "+r"(t.v[10]), "+r"(t.v[11]), "+r"(t.v[12]), "+r"(t.v[13]), "+r"(t.v[14]), "+r"(t.v[15])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[7]));
+  for (int i = 0; i < 8; i++) p0[i] = p2[i] = p1[i] = 0;
+  p1[8] = 0;
+  asm("add.cc.u32     %0, %5, %9;\n\t"
+      "addc.cc.u32    %1, %6, %10;\n\t"
+      "addc.cc.u32    %2, %7, %11;\n\t"
+      "addc.cc.u32    %3, %8, %12;\n\t"
+      "addc.u32       %4, 0, 0;"
+      : "=r"(sa[0]), "=r"(sa[1]), "=r"(sa[2]), "=r"(sa[3]), "=r"(ca)
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]));
+  asm("add.cc.u32     %0, %5, %9;\n\t"
+      "addc.cc.u32    %1, %6, %10;\n\t"
+      "addc.cc.u32    %2, %7, %11;\n\t"
+      "addc.cc.u32    %3, %8, %12;\n\t"
+      "addc.u32       %4, 0, 0;"
+      : "=r"(sb[0]), "=r"(sb[1]), "=r"(sb[2]), "=r"(sb[3]), "=r"(cb)
+      : "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p0[0]), "+r"(p0[1]), "+r"(p0[2]), "+r"(p0[3]), "+r"(p0[4])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p0[1]), "+r"(p0[2]), "+r"(p0[3]), "+r"(p0[4]), "+r"(p0[5])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[1]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p0[2]), "+r"(p0[3]), "+r"(p0[4]), "+r"(p0[5]), "+r"(p0[6])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[2]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p0[3]), "+r"(p0[4]), "+r"(p0[5]), "+r"(p0[6]), "+r"(p0[7])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[3]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p2[0]), "+r"(p2[1]), "+r"(p2[2]), "+r"(p2[3]), "+r"(p2[4])
+      : "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[4]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p2[1]), "+r"(p2[2]), "+r"(p2[3]), "+r"(p2[4]), "+r"(p2[5])
+      : "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[5]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p2[2]), "+r"(p2[3]), "+r"(p2[4]), "+r"(p2[5]), "+r"(p2[6])
+      : "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[6]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p2[3]), "+r"(p2[4]), "+r"(p2[5]), "+r"(p2[6]), "+r"(p2[7])
+      : "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(b[7]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p1[0]), "+r"(p1[1]), "+r"(p1[2]), "+r"(p1[3]), "+r"(p1[4])
+      : "r"(sa[0]), "r"(sa[1]), "r"(sa[2]), "r"(sa[3]), "r"(sb[0]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p1[1]), "+r"(p1[2]), "+r"(p1[3]), "+r"(p1[4]), "+r"(p1[5])
+      : "r"(sa[0]), "r"(sa[1]), "r"(sa[2]), "r"(sa[3]), "r"(sb[1]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p1[2]), "+r"(p1[3]), "+r"(p1[4]), "+r"(p1[5]), "+r"(p1[6])
+      : "r"(sa[0]), "r"(sa[1]), "r"(sa[2]), "r"(sa[3]), "r"(sb[2]));
+  asm("mad.lo.cc.u32  %0, %5, %9, %0;\n\t"
+      "madc.lo.cc.u32 %1, %6, %9, %1;\n\t"
+      "madc.lo.cc.u32 %2, %7, %9, %2;\n\t"
+      "madc.lo.cc.u32 %3, %8, %9, %3;\n\t"
+      "addc.u32       %4, %4, 0;\n\t"
+      "mad.hi.cc.u32  %1, %5, %9, %1;\n\t"
+      "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+      "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+      "madc.hi.u32    %4, %8, %9, %4;"
+      : "+r"(p1[3]), "+r"(p1[4]), "+r"(p1[5]), "+r"(p1[6]), "+r"(p1[7])
+      : "r"(sa[0]), "r"(sa[1]), "r"(sa[2]), "r"(sa[3]), "r"(sb[3]));
+  {
+    const uint32_t ma = 0u - ca, mb = 0u - cb;
+    const uint32_t x0 = sb[0] & ma, x1 = sb[1] & ma, x2 = sb[2] & ma, x3 = sb[3] & ma;
+    const uint32_t y0 = sa[0] & mb, y1 = sa[1] & mb, y2 = sa[2] & mb, y3 = sa[3] & mb;
+  asm("add.cc.u32     %0, %0, %6;\n\t"
+      "addc.cc.u32    %1, %1, %7;\n\t"
+      "addc.cc.u32    %2, %2, %8;\n\t"
+      "addc.cc.u32    %3, %3, %9;\n\t"
+      "addc.u32       %4, %4, %14;\n\t"
+      "add.cc.u32     %0, %0, %10;\n\t"
+      "addc.cc.u32    %1, %1, %11;\n\t"
+      "addc.cc.u32    %2, %2, %12;\n\t"
+      "addc.cc.u32    %3, %3, %13;\n\t"
+      "addc.u32       %4, %4, 0;"
+      : "+r"(p1[4]), "+r"(p1[5]), "+r"(p1[6]), "+r"(p1[7]), "+r"(p1[8])
+      : "r"(0u), "r"(x0), "r"(x1), "r"(x2), "r"(x3), "r"(y0), "r"(y1), "r"(y2), "r"(y3), "r"(ca & cb));
+  }
+  asm("sub.cc.u32     %0, %0, %9;\n\t"
+      "subc.cc.u32    %1, %1, %10;\n\t"
+      "subc.cc.u32    %2, %2, %11;\n\t"
+      "subc.cc.u32    %3, %3, %12;\n\t"
+      "subc.cc.u32    %4, %4, %13;\n\t"
+      "subc.cc.u32    %5, %5, %14;\n\t"
+      "subc.cc.u32    %6, %6, %15;\n\t"
+      "subc.cc.u32    %7, %7, %16;\n\t"
+      "subc.u32       %8, %8, 0;"
+      : "+r"(p1[0]), "+r"(p1[1]), "+r"(p1[2]), "+r"(p1[3]), "+r"(p1[4]), "+r"(p1[5]), "+r"(p1[6]), "+r"(p1[7]), "+r"(p1[8])
+      : "r"(p0[0]), "r"(p0[1]), "r"(p0[2]), "r"(p0[3]), "r"(p0[4]), "r"(p0[5]), "r"(p0[6]), "r"(p0[7]));
+  asm("sub.cc.u32     %0, %0, %9;\n\t"
+      "subc.cc.u32    %1, %1, %10;\n\t"
+      "subc.cc.u32    %2, %2, %11;\n\t"
+      "subc.cc.u32    %3, %3, %12;\n\t"
+      "subc.cc.u32    %4, %4, %13;\n\t"
+      "subc.cc.u32    %5, %5, %14;\n\t"
+      "subc.cc.u32    %6, %6, %15;\n\t"
+      "subc.cc.u32    %7, %7, %16;\n\t"
+      "subc.u32       %8, %8, 0;"
+      : "+r"(p1[0]), "+r"(p1[1]), "+r"(p1[2]), "+r"(p1[3]), "+r"(p1[4]), "+r"(p1[5]), "+r"(p1[6]), "+r"(p1[7]), "+r"(p1[8])
+      : "r"(p2[0]), "r"(p2[1]), "r"(p2[2]), "r"(p2[3]), "r"(p2[4]), "r"(p2[5]), "r"(p2[6]), "r"(p2[7]));
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    t.v[i] = p0[i];
+    t.v[8 + i] = p2[i];
+  }
+  asm("add.cc.u32     %0, %0, %12;\n\t"
+      "addc.cc.u32    %1, %1, %13;\n\t"
+      "addc.cc.u32    %2, %2, %14;\n\t"
+      "addc.cc.u32    %3, %3, %15;\n\t"
+      "addc.cc.u32    %4, %4, %16;\n\t"
+      "addc.cc.u32    %5, %5, %17;\n\t"
+      "addc.cc.u32    %6, %6, %18;\n\t"
+      "addc.cc.u32    %7, %7, %19;\n\t"
+      "addc.cc.u32    %8, %8, %20;\n\t"
+      "addc.cc.u32    %9, %9, 0;\n\t"
+      "addc.cc.u32    %10, %10, 0;\n\t"
+      "addc.u32       %11, %11, 0;"
+      : "+r"(t.v[4]), "+r"(t.v[5]), "+r"(t.v[6]), "+r"(t.v[7]), "+r"(t.v[8]), "+r"(t.v[9]), "+r"(t.v[10]), "+r"(t.v[11]), "+r"(t.v[12]), "+r"(t.v[13]), "+r"(t.v[14]), "+r"(t.v[15])
+      : "r"(p1[0]), "r"(p1[1]), "r"(p1[2]), "r"(p1[3]), "r"(p1[4]), "r"(p1[5]), "r"(p1[6]), "r"(p1[7]), "r"(p1[8]));
 }
 
 // t = a^2: off-diagonal products once, doubled, plus the diagonal
@@ -595,67 +653,65 @@ BG_DEV Fp<P> sqr_wide(const Fp<P>& a) {
   return redc<P>(t);
 }
 
-// a b - c d in Fq with one reduction
-BG_DEV Fq mul_sub_mul(const Fq& a, const Fq& b, const Fq& c, const Fq& d) {
-  Wide t, u;
+// Out-of-line pieces for the curve formulas.  Every Fq and Fq2 product of the MSM kernels is
+// made of three shared bodies (a 512-bit product, a 512-bit square, a reduction), so the hot
+// loops stay small in the instruction cache while squares use the squaring product and sums of
+// products share one reduction.
+static __device__ __noinline__ Wide wide_mul_ool(Fq a, Fq b) {
+  Wide t;
   wide_mul(t, a.v, b.v);
-  wide_add_2p2(t);
-  wide_mul(u, c.v, d.v);
-  wide_sub(t, u);
-  return redc<FqParams>(t);
+  return t;
 }
+static __device__ __noinline__ Wide wide_sqr_ool(Fq a) {
+  Wide t;
+  wide_sqr(t, a.v);
+  return t;
+}
+static __device__ __noinline__ Fq redc_ool(Wide t) { return redc<FqParams>(t); }
 
 // Fq2 product (Karatsuba) with two reductions:
 //   c0 = a0 b0 - a1 b1,  c1 = (a0 + a1)(b0 + b1) - a0 b0 - a1 b1 = a0 b1 + a1 b0
 // with the sums a0 + a1, b0 + b1 kept unreduced (below 2p) so that c1 is exact
-BG_DEV Fq2 fq2_mul_lazy(const Fq2& a, const Fq2& b) {
-  Wide t0, t1, t2;
-  wide_mul(t0, a.c0.v, b.c0.v);
-  wide_mul(t1, a.c1.v, b.c1.v);
-  uint32_t sa[8], sb[8];
-  raw_add8(sa, a.c0.v, a.c1.v);
-  raw_add8(sb, b.c0.v, b.c1.v);
-  wide_mul(t2, sa, sb);
+static __device__ __noinline__ Fq2 fq2_mul_ool(Fq2 a, Fq2 b) {
+  Wide t0 = wide_mul_ool(a.c0, b.c0);
+  const Wide t1 = wide_mul_ool(a.c1, b.c1);
+  Fq sa, sb;
+  raw_add8(sa.v, a.c0.v, a.c1.v);
+  raw_add8(sb.v, b.c0.v, b.c1.v);
+  Wide t2 = wide_mul_ool(sa, sb);
   wide_sub(t2, t0);
   wide_sub(t2, t1);
   wide_add_2p2(t0);
   wide_sub(t0, t1);
-  return {redc<FqParams>(t0), redc<FqParams>(t2)};
+  return {redc_ool(t0), redc_ool(t2)};
 }
 
 // a b - c d in Fq2 with two reductions (both components offset by 2 p^2, below 4 p^2)
-BG_DEV Fq2 fq2_mul_sub_mul(const Fq2& a, const Fq2& b, const Fq2& c, const Fq2& d) {
-  Wide re, im, w0, w1;
-  uint32_t s0[8], s1[8];
+static __device__ __noinline__ Fq2 fq2_mul_sub_mul_ool(Fq2 a, Fq2 b, Fq2 c, Fq2 d) {
+  Fq s0, s1;
   // a b: re = a0 b0 - a1 b1 + 2p^2, im = (a0 + a1)(b0 + b1) - a0 b0 - a1 b1 + 2p^2
-  wide_mul(re, a.c0.v, b.c0.v);
-  wide_mul(w1, a.c1.v, b.c1.v);
-  raw_add8(s0, a.c0.v, a.c1.v);
-  raw_add8(s1, b.c0.v, b.c1.v);
-  wide_mul(im, s0, s1);
+  Wide re = wide_mul_ool(a.c0, b.c0);
+  Wide w1 = wide_mul_ool(a.c1, b.c1);
+  raw_add8(s0.v, a.c0.v, a.c1.v);
+  raw_add8(s1.v, b.c0.v, b.c1.v);
+  Wide im = wide_mul_ool(s0, s1);
   wide_sub(im, re);
   wide_sub(im, w1);
   wide_add_2p2(im);
   wide_add_2p2(re);
   wide_sub(re, w1);
   // - c d: re += c1 d1 - c0 d0, im += c0 d0 + c1 d1 - (c0 + c1)(d0 + d1)
-  wide_mul(w0, c.c0.v, d.c0.v);
-  wide_mul(w1, c.c1.v, d.c1.v);
+  Wide w0 = wide_mul_ool(c.c0, d.c0);
+  w1 = wide_mul_ool(c.c1, d.c1);
   wide_add(re, w1);
   wide_sub(re, w0);
   wide_add(im, w0);
   wide_add(im, w1);
-  raw_add8(s0, c.c0.v, c.c1.v);
-  raw_add8(s1, d.c0.v, d.c1.v);
-  wide_mul(w0, s0, s1);
+  raw_add8(s0.v, c.c0.v, c.c1.v);
+  raw_add8(s1.v, d.c0.v, d.c1.v);
+  w0 = wide_mul_ool(s0, s1);
   wide_sub(im, w0);
-  return {redc<FqParams>(re), redc<FqParams>(im)};
+  return {redc_ool(re), redc_ool(im)};
 }
-
-// Out-of-line copies for the curve formulas (one body shared by every call site, as mul_ool)
-static __device__ __noinline__ Fq sqr_ool(Fq a) { return sqr_wide<FqParams>(a); }
-static __device__ __noinline__ Fq mul_sub_mul_ool(Fq a, Fq b, Fq c, Fq d) { return mul_sub_mul(a, b, c, d); }
-static __device__ __noinline__ Fq2 fq2_mul_ool(Fq2 a, Fq2 b) { return fq2_mul_lazy(a, b); }
-static __device__ __noinline__ Fq2 fq2_mul_sub_mul_ool(Fq2 a, Fq2 b, Fq2 c, Fq2 d) { return fq2_mul_sub_mul(a, b, c, d); }
 
 }  // namespace bg

@@ -631,12 +631,13 @@ template void msm_build_table<Fq>(cudaStream_t, const uint32_t*, size_t, MsmTabl
 template void msm_build_table<Fq2>(cudaStream_t, const uint32_t*, size_t, MsmTable&);
 
 template <class F>
-void msm_fetch(cudaStream_t st, MsmPlan& plan) {
+void msm_fetch(Ctx& ctx, cudaStream_t st, MsmPlan& plan) {
   constexpr int PW = 4 * FieldWords<F>::value;
   if (plan.W == 0) return;
   if (plan.fetch_stream) st = plan.fetch_stream;
   BG_CUDA(cudaMemcpyAsync(plan.host_window_sums, plan.d_window_sums,
                           (size_t)plan.W * plan.J * 2 * PW * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  ctx.d2h_bytes += (uint64_t)plan.W * plan.J * 2 * PW * sizeof(uint32_t);
 }
 
 // Window w = sum_j S_j + span * sum_j j R_j; total = sum_w 2^(c w) window_w (Horner).
@@ -678,8 +679,8 @@ template void msm_accumulate<Fq2>(Ctx&, cudaStream_t, const std::string&, const 
                                   cudaStream_t, const MsmTable*);
 template void msm_launch<Fq2>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const uint32_t*, size_t,
                               MsmPlan&, cudaStream_t, const MsmTable*);
-template void msm_fetch<Fq>(cudaStream_t, MsmPlan&);
-template void msm_fetch<Fq2>(cudaStream_t, MsmPlan&);
+template void msm_fetch<Fq>(Ctx&, cudaStream_t, MsmPlan&);
+template void msm_fetch<Fq2>(Ctx&, cudaStream_t, MsmPlan&);
 template void msm_finish<Fq>(const MsmPlan&, uint32_t*);
 template void msm_finish<Fq2>(const MsmPlan&, uint32_t*);
 

@@ -67,7 +67,7 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
                     MsmPlan& plan, cudaStream_t st_reduce = nullptr, const MsmTable* table = nullptr);
 // Enqueue the copy of the window sums to the host.
 template <class F>
-void msm_fetch(cudaStream_t st, MsmPlan& plan);
+void msm_fetch(Ctx& ctx, cudaStream_t st, MsmPlan& plan);
 // After the stream is synchronised: Horner over windows, affine result (packed words,
 // 16 for G1, 32 for G2; all zero = infinity).
 template <class F>

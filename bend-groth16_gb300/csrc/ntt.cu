@@ -187,6 +187,7 @@ static void upload_fes(Ctx& ctx, uint32_t* d, const std::vector<Fe>& v) {
   std::vector<uint32_t> words(v.size() * 8);
   for (size_t i = 0; i < v.size(); i++) bgh::fe_to_words32(words.data() + 8 * i, v[i]);
   BG_CUDA(cudaMemcpyAsync(d, words.data(), words.size() * 4, cudaMemcpyHostToDevice, ctx.stream));
+  ctx.h2d_bytes += words.size() * 4;
   BG_CUDA(cudaStreamSynchronize(ctx.stream));
 }
 

@@ -162,6 +162,7 @@ static void h2d(Ctx& ctx, int slot, void* dst, const void* src, size_t bytes, cu
   if (cudaPointerGetAttributes(&attr, src) == cudaSuccess) {
     if (attr.type == cudaMemoryTypeHost) {
       BG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+      ctx.h2d_bytes += bytes;
       return;
     }
     if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
@@ -170,6 +171,7 @@ static void h2d(Ctx& ctx, int slot, void* dst, const void* src, size_t bytes, cu
     }
   }
   cudaGetLastError();
+  ctx.h2d_bytes += bytes;
   // pageable source: stage in chunks through pinned memory
   const size_t chunk = 64ull << 20;
   char* pin = static_cast<char*>(ctx.pinned[slot].get(std::min(bytes, chunk) * 2));
@@ -226,6 +228,7 @@ static void upload_csr(Ctx& ctx, const void* src, uint32_t nc, CsrDev& out, cuda
 void check_status(Ctx& ctx, cudaStream_t st) {
   uint32_t s = 0;
   BG_CUDA(cudaMemcpyAsync(&s, ctx.d_status, 4, cudaMemcpyDeviceToHost, st));
+  ctx.d2h_bytes += 4;
   BG_CUDA(cudaStreamSynchronize(st));
   if (s) {
     BG_CUDA(cudaMemsetAsync(ctx.d_status, 0, 4, st));
@@ -422,10 +425,10 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     t_msm[jb.idx].start(acc_st);
     if (jb.g2) {
       msm_accumulate<Fq2>(ctx, acc_st, jb.tag, jb.pts, *so[j], p, red, jb.tab);
-      msm_fetch<Fq2>(acc_st, p);
+      msm_fetch<Fq2>(ctx, acc_st, p);
     } else {
       msm_accumulate<Fq>(ctx, acc_st, jb.tag, jb.pts, *so[j], p, red, jb.tab);
-      msm_fetch<Fq>(acc_st, p);
+      msm_fetch<Fq>(ctx, acc_st, p);
     }
     t_msm[jb.idx].stop(red);
   }

@@ -193,6 +193,9 @@ int bg_synth_square_chain(bg_ctx* ctx, uint32_t log2n, uint64_t seed, const char
 
 /* Window width c the MSM picks for n points (the tuning table), for reports. */
 int bg_msm_window_bits(size_t n);
+/* Window width c of the window tables a resident key (bg_pk_upload) builds for a query set of
+ * n points: one shared bucket set of 2^(c-1) buckets, floor(254 / c) + 1 table rows. */
+int bg_msm_table_window_bits(size_t n);
 
 /* ---- measurement (no counterpart in the reference, which prints only T lines) ------- */
 /* Enable (1) / disable (0) CUDA-event timing of the library's main kernels on the streams
@@ -202,6 +205,10 @@ int bg_ctx_profile(bg_ctx* ctx, int enable);
  * "msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_reduce_g1", "msm_reduce_g2", "msm_digits",
  * "msm_scatter", "ntt_pass".  Unknown names report zero launches. */
 int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms);
+/* Host <-> device bytes the context (and its batch lanes) copied since it was created: every
+ * upload of host data (files, witnesses, randomness, tables) and every download (MSM window
+ * sums, status words, results). */
+int bg_ctx_transfer_bytes(bg_ctx* ctx, uint64_t* h2d, uint64_t* d2h);
 /* Launch timeline: enable = 1 clears and starts recording the start and end of every timed
  * launch (the families above plus the proof phases); enable = 0 stops and writes one line
  * "family start_ms end_ms" per launch, in issue order, times relative to the first recorded
