@@ -444,13 +444,13 @@ int reduce_blocks_per_sm(uint32_t RT) {
   return cache[lrt];
 }
 template <class F>
-ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, int sm_count) {
+ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, int sm_count, uint32_t max_rt) {
   const double e = (double)entries / ((double)nb * sets);
   const double per_bucket = 2.0 + e / 32.0;
   ReduceShape best{nb < 32 ? nb : 32, 1, 1};
   best.J = nb / best.RT;
   double best_cost = 1e300;
-  for (uint32_t RT = 32; RT <= 256; RT <<= 1) {
+  for (uint32_t RT = 32; RT <= max_rt; RT <<= 1) {
     for (uint32_t M = 1; M <= 16; M <<= 1) {
       if ((uint64_t)RT * M > nb) continue;
       const uint32_t J = nb / (RT * M);
@@ -570,7 +570,11 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   }
   bucket_heavy<F>(prof, rs, so.offsets, buckets, bs);
 
-  const ReduceShape rsh = reduce_shape<F>(so.nb, so.sets, so.max_entries, ctx.sm_count);
+  // A reduction hidden under a later accumulation keeps its CTAs at 128 threads: a 256-thread
+  // CTA of ~210 registers leaves no room for an accumulation CTA on its SM for its whole
+  // (latency-bound) life (K = 18 proof: caps 64 / 128 / 256 measured 11.0 / 10.8 / 10.8 ms).
+  const ReduceShape rsh =
+      reduce_shape<F>(so.nb, so.sets, so.max_entries, ctx.sm_count, plan.latency_critical ? 256u : 128u);
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
   uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)so.sets * J * 2 * PW);
   {
@@ -752,7 +756,7 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   BG_CUDA(cudaGetDevice(&dev));
   BG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   msm_init_kernels();
-  const ReduceShape rsh = reduce_shape<Fq>(nb, W, max_entries, sms);
+  const ReduceShape rsh = reduce_shape<Fq>(nb, W, max_entries, sms, 256u);
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
   const unsigned tiles = ceil_div(nkeys + 1, kScanTile);
 

@@ -18,6 +18,10 @@ struct MsmPlan {
   // W XYZZ points after msm_fetch, in the context's pinned cache (a pageable destination
   // would make the copy block the host and serialise the streams of a proof)
   uint32_t* host_window_sums = nullptr;
+  // false: the reduction runs underneath later work (another MSM's accumulation) and takes
+  // small CTAs; true: it is the tail of the caller's critical path and takes the shape with
+  // the shortest dependent chain
+  bool latency_critical = true;
 };
 
 // Window table of a fixed point set: row w (w < W) holds 2^(c w) P_i for all i, so every

@@ -422,6 +422,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     const Job& jb = jobs[j];
     cudaStream_t red = ctx.side[1 + j];
     MsmPlan& p = plan[jb.idx];
+    p.latency_critical = j == 4;  // only msm_h's reduction is not hidden under an accumulation
     t_msm[jb.idx].start(acc_st);
     if (jb.g2) {
       msm_accumulate<Fq2>(ctx, acc_st, jb.tag, jb.pts, *so[j], p, red, jb.tab);
