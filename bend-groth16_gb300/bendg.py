@@ -36,7 +36,7 @@ EXPORTS = (
     "bg_repack_to_wire_dev", "bg_synth_square_chain", "bg_msm_window_bits", "bg_ctx_profile",
     "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch", "bg_prove_footprint",
     "bg_server_create", "bg_server_submit", "bg_server_wait", "bg_server_reserved_bytes", "bg_server_destroy",
-    "bg_ctx_timeline", "bg_msm_table_window_bits", "bg_ctx_transfer_bytes",
+    "bg_ctx_timeline", "bg_msm_table_window_bits", "bg_ctx_transfer_bytes", "bg_verify", "bg_pairing",
 )
 
 
@@ -55,6 +55,11 @@ class PhaseMs(ctypes.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name in PHASES}
+
+
+class Vk(ctypes.Structure):
+    _fields_ = [("alpha_g1", ctypes.c_void_p), ("beta_g2", ctypes.c_void_p), ("gamma_g2", ctypes.c_void_p),
+                ("delta_g2", ctypes.c_void_p), ("gamma_abc_g1", ctypes.c_void_p), ("n_ic", ctypes.c_size_t)]
 
 
 class Inputs(ctypes.Structure):
@@ -120,6 +125,8 @@ def lib():
                                  ctypes.POINTER(i32)]),
         "bg_server_reserved_bytes": (sz, [vp]),
         "bg_server_destroy": (None, [vp]),
+        "bg_verify": (i32, [ctypes.POINTER(Vk), vp, sz, ctypes.POINTER(Proof), ctypes.POINTER(i32)]),
+        "bg_pairing": (i32, [vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -136,6 +143,33 @@ def _ptr(a: np.ndarray):
 
 def _u32(a) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(a, dtype=np.uint32))
+
+
+def _noctx_check(st: int, what: str):
+    if st != 0:
+        msg = lib().bg_last_error(None)
+        raise BgError(st, "%s: %s" % (what, msg.decode() if msg else "error"))
+
+
+def verify(alpha_g1, beta_g2, gamma_g2, delta_g2, gamma_abc_g1, public, proof: Proof) -> bool:
+    """Groth16 verification on the host (bg_verify); points and public inputs in the wire
+    layout (uint32 words of 16-bit limbs, Montgomery), gamma_abc_g1 as (n_ic, 32) words"""
+    keep = [_u32(alpha_g1).reshape(-1), _u32(beta_g2).reshape(-1), _u32(gamma_g2).reshape(-1),
+            _u32(delta_g2).reshape(-1), _u32(gamma_abc_g1).reshape(-1), _u32(public).reshape(-1)]
+    n_ic = keep[4].size // 32
+    vk = Vk(*[_ptr(a) for a in keep[:5]], n_ic)
+    ok = ctypes.c_int()
+    _noctx_check(lib().bg_verify(ctypes.byref(vk), _ptr(keep[5]) if keep[5].size else None, keep[5].size // 16,
+                                 ctypes.byref(proof), ctypes.byref(ok)), "bg_verify")
+    return ok.value == 1
+
+
+def pairing(p_g1, q_g2) -> np.ndarray:
+    """e(P, Q) (bg_pairing): 192 uint32 words, 12 Fq elements in tower order, wire layout"""
+    p, q = _u32(p_g1).reshape(-1), _u32(q_g2).reshape(-1)
+    out = np.zeros(192, dtype=np.uint32)
+    _noctx_check(lib().bg_pairing(_ptr(p), _ptr(q), _ptr(out)), "bg_pairing")
+    return out
 
 
 # ---------------------------------------------------------------- wire-format helpers

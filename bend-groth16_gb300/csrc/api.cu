@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "pairing.hpp"
 #include "ec.cuh"
 #include "host_ff.hpp"
 #include "msm.h"
@@ -678,6 +679,29 @@ int bg_probe_imad(bg_ctx* ctx, int which, uint32_t iters, double* ops, double* m
 int bg_proof_format(const bg_proof* proof, char* buf, size_t buf_bytes) {
   if (!proof || !buf) return BG_E_ARG;
   return format_proof(proof, buf, buf_bytes);
+}
+
+int bg_verify(const bg_vk* vk, const uint32_t* public16, size_t n_public, const bg_proof* proof, int* valid) {
+  if (!vk || !proof || !valid) return BG_E_ARG;
+  try {
+    const bgh::VkWire w{vk->alpha_g1, vk->beta_g2, vk->gamma_g2, vk->delta_g2, vk->gamma_abc_g1, vk->n_ic};
+    *valid = bgh::groth16_verify(w, public16, n_public, proof->a, proof->b, proof->c);
+    return BG_OK;
+  } catch (const std::exception& e) {
+    bg::set_noctx_error(e.what());
+    return BG_E_ARG;
+  }
+}
+
+int bg_pairing(const uint32_t* p32, const uint32_t* q64, uint32_t* out192) {
+  if (!p32 || !q64 || !out192) return BG_E_ARG;
+  try {
+    bgh::pairing_wire(p32, q64, out192);
+    return BG_OK;
+  } catch (const std::exception& e) {
+    bg::set_noctx_error(e.what());
+    return BG_E_ARG;
+  }
 }
 
 }  // extern "C"

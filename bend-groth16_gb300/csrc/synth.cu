@@ -11,7 +11,9 @@
 //   h_query[k] = tau^k Z(tau)/delta G1 (k < d-1),
 //   l_query[j] = (beta A_{2+j} + alpha B_{2+j} + C_{2+j})(tau)/delta G1.
 // The trapdoor is also written to trapdoor.bin (5 canonical Fr, 16-bit-limb words) so tests
-// can check proofs without pairings.
+// can check proofs without pairings, and the verifying key to vk.bin (the .bin counterpart of
+// the reference's vk.json: alpha_g1, beta_g2, gamma_g2, delta_g2, u32 n_ic, n_ic IC points,
+// IC_i = (beta A_i + alpha B_i + C_i)(tau)/gamma G1 for the instance columns).
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -242,6 +244,14 @@ void synth_square_chain(Ctx& c, uint32_t log2n, uint64_t seed, const std::string
     v = bgh::fe_add(FR, v, C[2 + j]);
     kl[j] = canon(bgh::fe_mul(FR, v, dinv));
   }
+  // verifying key: IC_i = (beta A_i + alpha B_i + C_i)(tau) / gamma for the instance columns
+  const Fe ginv = bgh::fe_inv(FR, mont(gamma));
+  std::vector<Fe> kic(ni);
+  for (uint64_t i = 0; i < ni; i++) {
+    Fe v = bgh::fe_add(FR, bgh::fe_mul(FR, bm, A[i]), bgh::fe_mul(FR, am, B[i]));
+    v = bgh::fe_add(FR, v, C[i]);
+    kic[i] = canon(bgh::fe_mul(FR, v, ginv));
+  }
 
   // generators (canonical coordinates -> Montgomery)
   bgh::Aff<bgh::FqOps> g1;
@@ -268,6 +278,13 @@ void synth_square_chain(Ctx& c, uint32_t log2n, uint64_t seed, const std::string
   auto pl = device_fixed_base<Fq, bgh::FqOps>(c, t1, kl);
   auto pg1 = device_fixed_base<Fq, bgh::FqOps>(c, t1, {alpha, beta, delta});
   auto pg2 = device_fixed_base<Fq2, bgh::Fq2Ops>(c, t2, {beta, delta});
+  // vk.bin: alpha_g1, beta_g2, gamma_g2, delta_g2, u32 n_ic, IC_0 .. IC_{n_ic-1}
+  std::vector<uint32_t> vk = device_fixed_base<Fq, bgh::FqOps>(c, t1, {alpha});
+  const auto vk2 = device_fixed_base<Fq2, bgh::Fq2Ops>(c, t2, {beta, gamma, delta});
+  const auto vkic = device_fixed_base<Fq, bgh::FqOps>(c, t1, kic);
+  vk.insert(vk.end(), vk2.begin(), vk2.end());
+  vk.push_back(ni);
+  vk.insert(vk.end(), vkic.begin(), vkic.end());
 
   // CSR files: nnz; offsets[N+1]; (col, coeff = Montgomery one) per entry
   auto csr = [&](int which) {
@@ -303,6 +320,7 @@ void synth_square_chain(Ctx& c, uint32_t log2n, uint64_t seed, const std::string
   write_words(dir + "/pk_l.bin", pl);
   write_words(dir + "/rs.bin", rs);
   write_words(dir + "/trapdoor.bin", trap);
+  write_words(dir + "/vk.bin", vk);
 }
 
 }  // namespace bg

@@ -149,6 +149,30 @@ int bg_server_wait(bg_server* server, int timeout_ms, uint64_t* tag, bg_proof* o
                    double* latency_ms, double* queue_ms, int* status);
 size_t bg_server_reserved_bytes(bg_server* server);
 void bg_server_destroy(bg_server* server);
+/* ---- verification (the role of groth16-ref verify, ref/src/verify.rs:8-27) ------------- */
+/* Groth16 verifying key in the wire layout of the .bin files (16-bit limbs in u32 words,
+ * Montgomery coordinates, (0, 0) = infinity): alpha_g1 (32 words), beta_g2, gamma_g2,
+ * delta_g2 (64 words each), gamma_abc_g1 (n_ic x 32 words, n_ic = public inputs + 1).  The
+ * reference keeps it in vk.json; the .bin set has no vk file. */
+typedef struct bg_vk {
+  const uint32_t* alpha_g1;
+  const uint32_t* beta_g2;
+  const uint32_t* gamma_g2;
+  const uint32_t* delta_g2;
+  const uint32_t* gamma_abc_g1;
+  size_t n_ic;
+} bg_vk;
+/* *valid = 1 when e(A, B) = e(alpha, beta) e(vk_x, gamma) e(C, delta), vk_x = IC_0 +
+ * sum_i x_i IC_i, with every point on its curve and B in the order-r subgroup; 0 otherwise.
+ * public16: n_public Fr elements (wire layout, Montgomery; x_1.. of z), n_public = n_ic - 1
+ * (BG_E_ARG otherwise).  Host only (optimal ate pairing on the CPU, a few ms); needs no
+ * context or GPU. */
+int bg_verify(const bg_vk* vk, const uint32_t* public16, size_t n_public, const bg_proof* proof, int* valid);
+/* e(P, Q) for P in G1 (32 words) and Q in G2 (64 words), wire layout, written as 12 Fq elements
+ * (192 words) in tower order (Fq12 = Fq6[w]/(w^2 - v), Fq6 = Fq2[v]/(v^3 - (9 + u)));
+ * BG_E_ARG for points off their curve or outside the order-r subgroup.  Host only. */
+int bg_pairing(const uint32_t* p32, const uint32_t* q64, uint32_t* out192);
+
 /* Proof line text exactly as the reference prints it: "A x y\nB x0 x1 y0 y1\nC x y\n"
  * (canonical big-endian 0x + 64 hex digits, bend2/FORMAT.md:33).  buf needs >= 600 bytes. */
 int bg_proof_format(const bg_proof* proof, char* buf, size_t buf_bytes);
@@ -202,8 +226,9 @@ int bg_msm_table_window_bits(size_t n);
  * they run on; enabling clears earlier statistics. */
 int bg_ctx_profile(bg_ctx* ctx, int enable);
 /* Launch count and summed device time (ms) of one kernel family since profiling was enabled:
- * "msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_reduce_g1", "msm_reduce_g2", "msm_digits",
- * "msm_scatter", "ntt_pass".  Unknown names report zero launches. */
+ * "msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_heavy_g1", "msm_heavy_g2", "msm_reduce_g1",
+ * "msm_reduce_g2", "msm_digits", "msm_scatter", "ntt_pass", "evals", "qap".  Unknown names report
+ * zero launches. */
 int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms);
 /* Host <-> device bytes the context (and its batch lanes) copied since it was created: every
  * upload of host data (files, witnesses, randomness, tables) and every download (MSM window

@@ -733,6 +733,14 @@ int bgo_synth_square_chain(uint32_t log2n, uint64_t seed, const char *dir, int t
     v = f_add(&FR, v, C[2 + j]);
     kl[j] = f_from_mont(&FR, f_mul(&FR, v, dinv));
   }
+  /* verifying key: IC_i = (beta A_i + alpha B_i + C_i)(tau) / gamma for the instance columns */
+  fe ginv = f_inv(&FR, f_to_mont(&FR, gamma));
+  fe kic[2];
+  for (uint64_t i = 0; i < ni; i++) {
+    fe v = f_add(&FR, f_mul(&FR, bm, A[i]), f_mul(&FR, am, B[i]));
+    v = f_add(&FR, v, C[i]);
+    kic[i] = f_from_mont(&FR, f_mul(&FR, v, ginv));
+  }
   free(wk); free(den); free(A); free(B); free(C);
 
   /* fixed-base tables T[w][d-1] = d 2^(8w) G */
@@ -761,11 +769,16 @@ int bgo_synth_square_chain(uint32_t log2n, uint64_t seed, const char *dir, int t
     }
     for (int i = 0; i < 8; i++) { b1 = g1_dbl(b1); b2 = g2_dbl(b2); }
   }
-  fe kg1[3] = {alpha, beta, delta}, kg2[2] = {beta, delta};
-  struct { const fe *k; size_t n; int g2; const char *name; } outs[7] = {
+  fe kg1[3] = {alpha, beta, delta}, kg2[2] = {beta, delta}, kvk1[1] = {alpha}, kvk2[3] = {beta, gamma, delta};
+  struct { const fe *k; size_t n; int g2; const char *name; } outs[10] = {
       {ka, m, 0, "pk_a"}, {kb, m, 0, "pk_b1"}, {kb, m, 1, "pk_b2"}, {kh, d - 1, 0, "pk_h"},
-      {kl, nw, 0, "pk_l"}, {kg1, 3, 0, "pk_g1"}, {kg2, 2, 1, "pk_g2"}};
-  for (int o = 0; o < 7; o++) {
+      {kl, nw, 0, "pk_l"}, {kg1, 3, 0, "pk_g1"}, {kg2, 2, 1, "pk_g2"},
+      {kvk1, 1, 0, NULL}, {kvk2, 3, 1, NULL}, {kic, ni, 0, NULL}};
+  /* vk.bin: alpha_g1, beta_g2, gamma_g2, delta_g2, u32 n_ic, IC_0 .. IC_{n_ic-1} */
+  uint32_t vk[32 + 3 * 64 + 1 + 2 * 32];
+  size_t vk_off[3] = {0, 32, 32 + 3 * 64 + 1};
+  vk[32 + 3 * 64] = (uint32_t)ni;
+  for (int o = 0; o < 10; o++) {
     size_t n = outs[o].n;
     size_t pw = outs[o].g2 ? 64 : 32;
     void *pts = malloc((outs[o].g2 ? sizeof(g2_aff) : sizeof(g1_aff)) * (n ? n : 1));
@@ -780,7 +793,8 @@ int bgo_synth_square_chain(uint32_t log2n, uint64_t seed, const char *dir, int t
         if (a.inf) memset(wbuf + pw * i, 0, 4 * pw); else g1_write16(wbuf + pw * i, &a);
       }
     }
-    bad |= write_u32(dir, outs[o].name, wbuf, pw * n);
+    if (outs[o].name) bad |= write_u32(dir, outs[o].name, wbuf, pw * n);
+    else memcpy(vk + vk_off[o - 7], wbuf, 4 * pw * n);
     free(wbuf);
     free(pts);
   }
@@ -810,5 +824,6 @@ int bgo_synth_square_chain(uint32_t log2n, uint64_t seed, const char *dir, int t
   fe tv[5] = {tau, alpha, beta, gamma, delta};
   for (int i = 0; i < 5; i++) fe_write16(trap + 16 * i, tv[i]);
   bad |= write_u32(dir, "trapdoor", trap, 80);
+  bad |= write_u32(dir, "vk", vk, sizeof(vk) / 4);
   return bad;
 }

@@ -141,3 +141,23 @@ def test_degenerate_witness_matches_c_oracle(ctx, tmp_path, x0):
         proof, _ = key.prove(files.words("witness"), files.words("rs"))
         assert np.array_equal(proof_words(proof), want)
     key.release()
+
+
+@pytest.mark.parametrize("log2n", [12, 16])
+def test_gpu_proofs_verify(ctx, tmp_path, log2n):
+    """proofs from every entry point pass the pairing verifier under the instance's vk.bin"""
+    from test_verify import read_vk, proof_from_words
+    path = str(tmp_path / "sq")
+    ctx.synth_square_chain(log2n, 555 + log2n, path)
+    vk = read_vk(path)
+    files = bendg.HostFiles(path)
+    pub = files.words("witness")[16:32]
+    proof, _ = ctx.prove_dir(path)
+    assert bendg.verify(*vk, pub, proof)
+    key = ctx.pk_upload(files)
+    proof, _ = key.prove(files.words("witness"), files.words("rs"))
+    key.release()
+    assert bendg.verify(*vk, pub, proof)
+    w = proof_words(proof).copy()
+    w[0:32], w[96:128] = w[96:128].copy(), w[0:32].copy()  # A and C swapped
+    assert not bendg.verify(*vk, pub, proof_from_words(w))
