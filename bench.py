@@ -120,12 +120,12 @@ def ensure_instance(args, dist: Dist, generator) -> str:
 
 
 def window_counts(L, n):
-    c = L.bg_msm_window_bits(n)
+    c = L.bg_msm_window_bits(n, 0)
     return c, 254 // c + 1
 
 
-def table_window_counts(L, n):
-    c = L.bg_msm_table_window_bits(n)
+def table_window_counts(L, n, curve=0):
+    c = L.bg_msm_table_window_bits(n, curve)
     return c, 254 // c + 1
 
 
@@ -246,7 +246,7 @@ def run_ours(args, dist: Dist):
     g1_sizes = [na, nb, nh, nl]
     # the timed proofs run against the resident key: window tables, W = floor(254 / c_table) + 1
     entries_g1 = sum(n * table_window_counts(L, n)[1] for n in g1_sizes)
-    entries_g2 = nb * table_window_counts(L, nb)[1]
+    entries_g2 = nb * table_window_counts(L, nb, 1)[1]
     work = {"msm_bucket_acc_g1": entries_g1 * MADD_G1_IMAD,
             "msm_bucket_acc_g2": entries_g2 * MADD_G2_IMAD}
     roof = None
@@ -309,7 +309,8 @@ def run_ours(args, dist: Dist):
                    "log2_constraints": args.log2n, "domain_log2": lg, "n_a": na, "n_b": nb, "n_h": nh, "n_l": nl,
                    "seed": args.seed, "parallelism": "replicas" if dist.world > 1 else "single GPU",
                    "l2": "flushed (512 MiB write) before every timed step",
-                   "msm_window_bits": {str(n): L.bg_msm_table_window_bits(n) for n in sorted(set(g1_sizes + [nb]))},
+                   "msm_window_bits": {"g1": {str(n): L.bg_msm_table_window_bits(n, 0) for n in sorted(set(g1_sizes))},
+                                       "g2": {str(nb): L.bg_msm_table_window_bits(nb, 1)}},
                    "msm_layout": "resident key: 2^(c w) window tables, one shared bucket set per MSM"},
         "proof_verified": bool(verified),
         "e2e": e2e, "roofline": roof_iso or roof, "roofline_in_proof": roof, "gpu_launches": int(launches), "clocks": clk,
@@ -431,6 +432,33 @@ def percentile(xs, q):
     return s[i]
 
 
+def single_proofs(ctx, key, path, reps=5):
+    """BASELINE configuration 2 at its larger size: plain one-at-a-time proofs against a
+    resident key (wall time of the synchronous call, device work included), and the pairing
+    check of the last one under the instance's vk.bin"""
+    import numpy as np
+
+    import bendg
+    f = bendg.HostFiles(path, pinned=True)
+    w, rs = f.words("witness"), f.words("rs")
+    for _ in range(2):
+        key.prove(w, rs)
+    walls, phases = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        proof, t = key.prove(w, rs)
+        walls.append((time.perf_counter() - t0) * 1e3)
+        phases.append(t)
+    vkw = np.fromfile(os.path.join(path, "vk.bin"), dtype="<u4").astype(np.uint32)
+    n_ic = int(vkw[224])
+    ok = bendg.verify(vkw[0:32], vkw[32:96], vkw[96:160], vkw[160:224], vkw[225:225 + 32 * n_ic],
+                      w[16:16 * n_ic], proof)
+    hdr = f.words("header")
+    return {"log2_constraints": int(hdr[0]).bit_length() - 1, "ms_per_proof": round(statistics.median(walls), 3),
+            "phases_ms_median": {k: round(statistics.median(p[k] for p in phases), 3) for k in phases[0]},
+            "proof_verified": bool(ok), "timing": "wall clock of bg_prove_resident, median of %d" % reps}
+
+
 def serving(ctx, args, lanes=8, seconds=1.5):
     """BASELINE configuration 4: Poisson arrivals of prove requests with K drawn from
     SERVE_KS, all five proving keys resident, continuous batching in the library's server;
@@ -440,7 +468,7 @@ def serving(ctx, args, lanes=8, seconds=1.5):
 
     import bendg
     rng = random.Random(args.seed + 4)
-    keys, pools = {}, {}
+    keys, pools, paths = {}, {}, {}
     for k in SERVE_KS:
         a = argparse.Namespace(**vars(args))
         a.log2n = k
@@ -451,7 +479,9 @@ def serving(ctx, args, lanes=8, seconds=1.5):
         keys[k] = ctx.pk_upload(f)
         z = f.words("witness").copy()
         pools[k] = [shifted_witness(z, 1 + j) for j in range(4)]  # distinct valid witnesses
+        paths[k] = path
         del f
+    k20 = single_proofs(ctx, keys[SERVE_KS[-1]], paths[SERVE_KS[-1]])
     budget = 64 << 30
     srv = bendg.Server(ctx, lanes=lanes, hbm_budget_bytes=budget)
     # warm every lane on the largest key
@@ -506,7 +536,8 @@ def serving(ctx, args, lanes=8, seconds=1.5):
         keys[k].release()
     return {"workload": "Poisson arrivals, K drawn from %s with weights %s (seed %d), %s s of arrivals per rate, "
                         "all five keys resident" % (list(SERVE_KS), list(SERVE_WEIGHTS), args.seed + 4, seconds),
-            "lanes": lanes, "hbm_budget_bytes": budget, "reserved_scratch_bytes": reserved, "rates": results}
+            "lanes": lanes, "hbm_budget_bytes": budget, "reserved_scratch_bytes": reserved, "rates": results,
+            "single_proof_k20": k20}
 
 
 def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):

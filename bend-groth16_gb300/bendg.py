@@ -37,6 +37,7 @@ EXPORTS = (
     "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch", "bg_prove_footprint",
     "bg_server_create", "bg_server_submit", "bg_server_wait", "bg_server_reserved_bytes", "bg_server_destroy",
     "bg_ctx_timeline", "bg_msm_table_window_bits", "bg_ctx_transfer_bytes", "bg_verify", "bg_pairing",
+    "bg_msm_window_override",
 )
 
 
@@ -107,8 +108,9 @@ def lib():
         "bg_repack_to_packed_dev": (i32, [vp, vp, vp, sz]),
         "bg_repack_to_wire_dev": (i32, [vp, vp, vp, sz]),
         "bg_synth_square_chain": (i32, [vp, u32, u64, ctypes.c_char_p]),
-        "bg_msm_window_bits": (i32, [sz]),
-        "bg_msm_table_window_bits": (i32, [sz]),
+        "bg_msm_window_bits": (i32, [sz, i32]),
+        "bg_msm_table_window_bits": (i32, [sz, i32]),
+        "bg_msm_window_override": (i32, [vp, i32, i32, i32]),
         "bg_ctx_profile": (i32, [vp, i32]),
         "bg_ctx_timeline": (i32, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "bg_ctx_transfer_bytes": (i32, [vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
@@ -229,6 +231,11 @@ class Context:
 
     def profile(self, enable: bool):
         self._check(self._L.bg_ctx_profile(self.h, 1 if enable else 0), "bg_ctx_profile")
+
+    def window_override(self, layout: int, curve: int, c: int):
+        """force the MSM window width (layout 0: bucket set per window, 1: tables of keys uploaded
+        afterwards); c = 0 restores the library's choice"""
+        self._check(self._L.bg_msm_window_override(self.h, layout, curve, c), "bg_msm_window_override")
 
     def transfer_bytes(self):
         """(host-to-device, device-to-host) bytes copied by this context so far"""

@@ -117,6 +117,7 @@ void msm_host(Ctx& c, const uint32_t* points16, const uint32_t* scalars16, size_
     // scalars are canonical: repack without a Montgomery conversion
     const uint32_t* sc = stage_in(c, "api.msm_sc", scalars16, n);
     MsmPlan plan;
+    plan.c = c.c_override[0][FieldWords<F>::value == 16 ? 1 : 0];
     msm_launch<F>(c, c.stream, "api.msm", pts, sc, n, plan);
     msm_fetch<F>(c, c.stream, plan);
     BG_CUDA(cudaStreamSynchronize(c.stream));
@@ -134,6 +135,7 @@ void msm_dev(Ctx& c, const uint32_t* d_points, const uint32_t* d_scalars, size_t
     return;
   }
   MsmPlan plan;
+  plan.c = c.c_override[0][FieldWords<F>::value == 16 ? 1 : 0];
   msm_launch<F>(c, c.stream, "api.msm", d_points, d_scalars, n, plan);
   msm_fetch<F>(c, c.stream, plan);
   BG_CUDA(cudaStreamSynchronize(c.stream));
@@ -278,8 +280,16 @@ void bg_host_free(void* p) {
   if (p) cudaFreeHost(p);
 }
 
-int bg_msm_window_bits(size_t n) { return msm_pick_c(n); }
-int bg_msm_table_window_bits(size_t n) { return msm_pick_c_table(n); }
+int bg_msm_window_bits(size_t n, int curve) { return msm_pick_c(n, curve == BG_CURVE_G2); }
+int bg_msm_table_window_bits(size_t n, int curve) { return msm_pick_c_table(n, curve == BG_CURVE_G2); }
+
+int bg_msm_window_override(bg_ctx* ctx, int layout, int curve, int c) {
+  if (!ctx || (layout != 0 && layout != 1) || (curve != BG_CURVE_G1 && curve != BG_CURVE_G2) ||
+      (c != 0 && (c < 2 || c > 22)))
+    return BG_E_ARG;
+  ctx->c.c_override[layout][curve == BG_CURVE_G2 ? 1 : 0] = c;
+  return BG_OK;
+}
 
 int bg_msm_g1(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, size_t n, uint32_t* out_jac16) {
   if (!ctx || !out_jac16 || (n && (!points16 || !scalars16))) return BG_E_ARG;

@@ -148,6 +148,9 @@ struct Ctx {
   std::string last_error;
   uint32_t* d_status = nullptr;           // device-side error flags (see BG_DSTATUS_*)
   uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host <-> device bytes this context has copied
+  // window widths forced for tuning (bg_msm_window_override): [0] per-window bucket sets,
+  // [1] window tables of keys uploaded afterwards; [curve]; 0 = the library's choice
+  int c_override[2][2] = {{0, 0}, {0, 0}};
   std::map<int, NttTables> ntt_tabs;      // per domain size, built on first use
   // optional per-kernel timing: CUDA events recorded around selected launches on their
   // own stream, resolved when the statistics are read

@@ -24,6 +24,7 @@
 #include "ec.cuh"
 #include "host_ff.hpp"
 #include "msm.h"
+#include "msm_tune.h"
 
 #include <cmath>
 #include <cstring>
@@ -470,10 +471,19 @@ ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, int sm_count, ui
 }
 
 // ---------------------------------------------------------------- host driver
-int msm_pick_c(size_t n) {
+static int floor_log2(size_t n) {
   int lg = 0;
   while ((size_t(1) << (lg + 1)) <= n) lg++;
-  int c = lg - 3;
+  return lg;
+}
+static int tuned(const signed char (*tab)[kTuneMaxLog2 - kTuneMinLog2 + 1], size_t n, bool g2) {
+  const int lg = floor_log2(n);
+  return lg >= kTuneMinLog2 && lg <= kTuneMaxLog2 ? tab[g2 ? 1 : 0][lg - kTuneMinLog2] : 0;
+}
+
+int msm_pick_c(size_t n, bool g2) {
+  if (const int t = tuned(kTuneSets, n, g2)) return t;
+  int c = floor_log2(n) - 3;
   if (c < 3) c = 3;
   if (c > 16) c = 16;
   return c;
@@ -594,28 +604,28 @@ template <class F>
 void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_t* d_points,
                 const uint32_t* d_scalars, size_t n, MsmPlan& plan, cudaStream_t st_reduce, const MsmTable* table) {
   if (table && table->n != n) throw Error(BG_E_ARG, "msm: window table built for another size");
-  const int c = table ? table->c : (plan.c > 0 ? plan.c : msm_pick_c(n));
+  const int c = table ? table->c : (plan.c > 0 ? plan.c : msm_pick_c(n, FieldWords<F>::value == 16));
   MsmSort so;
   msm_sort(ctx, st, tag, d_scalars, n, c, table != nullptr, so);
   so.done = nullptr;  // same stream: already ordered
   msm_accumulate<F>(ctx, st, tag, d_points, so, plan, st_reduce, table);
 }
 
-int msm_pick_c_table(size_t n) {
+int msm_pick_c_table(size_t n, bool g2) {
   // one shared bucket set: wider windows (fewer additions) at the price of 2^(c-1) buckets
-  int lg = 0;
-  while ((size_t(1) << (lg + 1)) <= n) lg++;
-  int c = lg - 1;
+  if (const int t = tuned(kTuneTables, n, g2)) return t;
+  int c = floor_log2(n) - 1;
   if (c < 6) c = 6;
   if (c > 18) c = 18;
   return c;
 }
 
 template <class F>
-void msm_build_table(cudaStream_t st, const uint32_t* d_points, size_t n, MsmTable& t) {
+void msm_build_table(cudaStream_t st, const uint32_t* d_points, size_t n, MsmTable& t, int c) {
   constexpr int PW = 2 * FieldWords<F>::value;
+  if (c != 0 && (c < 2 || c > 22)) throw Error(BG_E_ARG, "msm table: window width out of range");
   t.n = n;
-  t.c = msm_pick_c_table(n);
+  t.c = c ? c : msm_pick_c_table(n, FieldWords<F>::value == 16);
   t.W = 254 / t.c + 1;
   if (n == 0) return;
   if (n * (size_t)t.W >= 0x80000000ull) throw Error(BG_E_ARG, "msm table: n x windows must be below 2^31");
@@ -631,8 +641,8 @@ void msm_build_table(cudaStream_t st, const uint32_t* d_points, size_t n, MsmTab
   BG_CHECK_LAUNCH();
 }
 
-template void msm_build_table<Fq>(cudaStream_t, const uint32_t*, size_t, MsmTable&);
-template void msm_build_table<Fq2>(cudaStream_t, const uint32_t*, size_t, MsmTable&);
+template void msm_build_table<Fq>(cudaStream_t, const uint32_t*, size_t, MsmTable&, int);
+template void msm_build_table<Fq2>(cudaStream_t, const uint32_t*, size_t, MsmTable&, int);
 
 template <class F>
 void msm_fetch(Ctx& ctx, cudaStream_t st, MsmPlan& plan) {
@@ -711,7 +721,7 @@ namespace bg {
 namespace {
 
 constexpr size_t kNoAllocMaxPoints = size_t(1) << 14;
-constexpr size_t kNoAllocScratchBytes = size_t(9) << 20;  // the 2^14-point worst case needs 8.2 MiB
+constexpr size_t kNoAllocScratchBytes = size_t(9) << 20;  // the worst case up to 2^14 points needs 6.6 MiB
 constexpr size_t kNoAllocHostWords = 8192;                // window parts copied back for the Horner
 constexpr int kNoAllocMaxDevices = 64;
 

@@ -45,12 +45,14 @@ struct MsmSort {
   cudaEvent_t done = nullptr;   // recorded after the scatter (null: ordered by the stream)
 };
 
-int msm_pick_c(size_t n);
-int msm_pick_c_table(size_t n);
+// window width for n points (the committed table of msm_tune.h, else a size rule)
+int msm_pick_c(size_t n, bool g2 = false);
+int msm_pick_c_table(size_t n, bool g2 = false);
 void msm_init_kernels();
-// allocate t.d (cudaMalloc) and fill it from n packed affine points on `st`
+// allocate t.d (cudaMalloc) and fill it from n packed affine points on `st`; c = 0 picks the
+// window width from n
 template <class F>
-void msm_build_table(cudaStream_t st, const uint32_t* d_points, size_t n, MsmTable& t);
+void msm_build_table(cudaStream_t st, const uint32_t* d_points, size_t n, MsmTable& t, int c = 0);
 void exclusive_scan(Workspace& ws, const std::string& tag, const uint32_t* d_in, uint32_t* d_out, size_t n,
                     cudaStream_t st, int depth);
 

@@ -263,11 +263,11 @@ PkDev* pk_upload(Ctx& ctx, const bg_inputs& in, bool build_tables) {
     pk->beta2 = host_affine_from_wire<Fq2Ops>(g2);
     pk->delta2 = host_affine_from_wire<Fq2Ops>(g2 + 64);
     if (build_tables) {
-      msm_build_table<Fq>(st, pk->pa, h.na, pk->tab[0]);
-      msm_build_table<Fq>(st, pk->pb1, h.nb, pk->tab[1]);
-      msm_build_table<Fq2>(st, pk->pb2, h.nb, pk->tab[2]);
-      msm_build_table<Fq>(st, pk->ph, h.nh, pk->tab[3]);
-      msm_build_table<Fq>(st, pk->pl, h.nl, pk->tab[4]);
+      msm_build_table<Fq>(st, pk->pa, h.na, pk->tab[0], ctx.c_override[1][0]);
+      msm_build_table<Fq>(st, pk->pb1, h.nb, pk->tab[1], ctx.c_override[1][0]);
+      msm_build_table<Fq2>(st, pk->pb2, h.nb, pk->tab[2], ctx.c_override[1][1]);
+      msm_build_table<Fq>(st, pk->ph, h.nh, pk->tab[3], ctx.c_override[1][0]);
+      msm_build_table<Fq>(st, pk->pl, h.nl, pk->tab[4], ctx.c_override[1][0]);
       pk->tables = true;
     }
     check_status(ctx, st);
@@ -407,7 +407,8 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   std::vector<std::pair<SortKey, MsmSort>> sorts;
   sorts.reserve(5);
   auto sort_for = [&](const Job& jb, cudaStream_t s) -> const MsmSort& {
-    const SortKey k{jb.sc, jb.n, jb.tab ? jb.tab->c : msm_pick_c(jb.n), jb.tab != nullptr};
+    const int c_sets = ctx.c_override[0][jb.g2 ? 1 : 0] ? ctx.c_override[0][jb.g2 ? 1 : 0] : msm_pick_c(jb.n, jb.g2);
+    const SortKey k{jb.sc, jb.n, jb.tab ? jb.tab->c : c_sets, jb.tab != nullptr};
     for (auto& e : sorts)
       if (e.first.sc == k.sc && e.first.n == k.n && e.first.c == k.c && e.first.shared == k.shared) return e.second;
     sorts.emplace_back(k, MsmSort());
@@ -500,7 +501,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
 // prove_resident request), used for admission control; a 10% margin covers rounding.
 static size_t msm_footprint(size_t n, bool g2) {
   if (n == 0) return 0;
-  const int c = msm_pick_c(n);
+  const int c = msm_pick_c(n, g2);
   const size_t W = 254 / c + 1, nb = size_t(1) << (c - 1), nkeys = W * nb;
   const size_t PW = g2 ? 64 : 32, K = 32;
   const size_t entries = n * W, threads = (entries + K - 1) / K;

@@ -215,11 +215,16 @@ int bg_repack_to_wire_dev(bg_ctx* ctx, const uint32_t* d_packed, uint32_t* d_wir
  * fixed-base multiplications run on the device.  Produces inputs only; not part of proving. */
 int bg_synth_square_chain(bg_ctx* ctx, uint32_t log2n, uint64_t seed, const char* dir);
 
-/* Window width c the MSM picks for n points (the tuning table), for reports. */
-int bg_msm_window_bits(size_t n);
+/* Window width c the MSM picks for n points of `curve` (BG_CURVE_G1/G2) with one bucket set
+ * per window: the committed tuning table (bend-groth16_gb300/csrc/msm_tune.h), else a size rule. */
+int bg_msm_window_bits(size_t n, int curve);
 /* Window width c of the window tables a resident key (bg_pk_upload) builds for a query set of
  * n points: one shared bucket set of 2^(c-1) buckets, floor(254 / c) + 1 table rows. */
-int bg_msm_table_window_bits(size_t n);
+int bg_msm_table_window_bits(size_t n, int curve);
+/* Tuning hook: force the window width of later MSMs of this context, layout 0 = one bucket set
+ * per window (bg_msm_*, one-shot proofs), 1 = window tables of keys uploaded afterwards;
+ * c = 0 restores the library's choice, else 2..22. */
+int bg_msm_window_override(bg_ctx* ctx, int layout, int curve, int c);
 
 /* ---- measurement (no counterpart in the reference, which prints only T lines) ------- */
 /* Enable (1) / disable (0) CUDA-event timing of the library's main kernels on the streams

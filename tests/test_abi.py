@@ -28,4 +28,5 @@ def test_status_strings(built_lib):
     L = bendg.lib()
     for st in range(7):
         assert L.bg_strerror(st)
-    assert L.bg_msm_window_bits(1 << 20) >= L.bg_msm_window_bits(1 << 10)
+    assert L.bg_msm_window_bits(1 << 20, 0) >= L.bg_msm_window_bits(1 << 10, 0)
+    assert L.bg_msm_table_window_bits(1 << 18, 1) >= L.bg_msm_table_window_bits(1 << 10, 1)

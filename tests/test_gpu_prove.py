@@ -91,7 +91,7 @@ def test_synth_gpu_equals_cpu(ctx, tmp_path):
         assert open(g / f, "rb").read() == open(c / f, "rb").read(), f
 
 
-@pytest.mark.parametrize("log2n", [14, 18])
+@pytest.mark.parametrize("log2n", [14, 18, 20])
 def test_prove_matches_c_oracle(ctx, tmp_path, log2n):
     """full-size proof bit-identical to the C oracle's on the same synthetic instance"""
     import oracle_c
