@@ -162,6 +162,7 @@ void ctx_init(Ctx& c, int device) {
   int least = 0, greatest = 0;
   BG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
   BG_CUDA(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking, greatest));
+  BG_CUDA(cudaStreamCreateWithPriority(&c.copy, cudaStreamNonBlocking, least));
   for (int i = 0; i < kStreams; i++) {
     BG_CUDA(cudaStreamCreateWithPriority(&c.side[i], cudaStreamNonBlocking, i == 0 ? least : greatest));
     BG_CUDA(cudaEventCreateWithFlags(&c.ev_join[i], cudaEventDisableTiming));
@@ -175,6 +176,11 @@ void ctx_init(Ctx& c, int device) {
 void ctx_release(Ctx& c) {
   cudaSetDevice(c.device);
   if (c.stream) cudaStreamSynchronize(c.stream);
+  if (c.copy) {
+    cudaStreamSynchronize(c.copy);
+    cudaStreamDestroy(c.copy);
+    c.copy = nullptr;
+  }
   for (int i = 0; i < kStreams; i++) {
     if (c.side[i]) {
       cudaStreamSynchronize(c.side[i]);
@@ -521,7 +527,7 @@ int bg_prove_host(bg_ctx* ctx, const bg_inputs* in, bg_proof* out, bg_phase_ms* 
     const auto t0 = std::chrono::steady_clock::now();
     const Header h = parse_header(*in);
     validate_inputs(*in, h, true);
-    PkDev* pk = pk_upload(ctx->c, *in, false);
+    PkDev* pk = pk_stage_oneshot(ctx->c, *in);
     const double up_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     try {
       prove_resident(ctx->c, *pk, static_cast<const uint32_t*>(in->witness), static_cast<const uint32_t*>(in->rs),
@@ -559,7 +565,7 @@ int bg_prove_dir(bg_ctx* ctx, const char* dir, bg_proof* out, bg_phase_ms* times
     cudaSetDevice(ctx->c.device);
     const Header h = parse_header(in);
     validate_inputs(in, h, true);
-    PkDev* pk = pk_upload(ctx->c, in, false);
+    PkDev* pk = pk_stage_oneshot(ctx->c, in);
     const double load_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     try {
       prove_resident(ctx->c, *pk, static_cast<const uint32_t*>(in.witness), static_cast<const uint32_t*>(in.rs),

@@ -140,6 +140,7 @@ struct Ctx {
   int sm_count = 0;
   cudaStream_t stream = nullptr;          // main stream: every public call is ordered on it
   cudaStream_t side[kStreams] = {};       // concurrent MSMs inside a proof
+  cudaStream_t copy = nullptr;            // uploads that overlap a proof (one-shot keys)
   cudaEvent_t ev_fork = nullptr;
   cudaEvent_t ev_join[kStreams] = {};
   Workspace ws;

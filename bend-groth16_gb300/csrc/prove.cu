@@ -200,22 +200,30 @@ static void h2d(Ctx& ctx, int slot, void* dst, const void* src, size_t bytes, cu
   cudaEventDestroy(done[1]);
 }
 
+// device buffer: cudaMalloc'd (owned by the key) or, for pooled one-shot keys, the context's
+// workspace slot `tag` (kept for the next proof)
+static void* key_alloc(Ctx& ctx, bool pooled, const std::string& tag, size_t bytes) {
+  if (pooled) return ctx.ws.get_t<uint32_t>("oneshot." + tag, (bytes + 3) / 4);
+  return dmalloc(bytes);
+}
+
 static void upload_points(Ctx& ctx, const void* src, size_t n, int words_per_point, uint32_t*& d_out,
-                          cudaStream_t st) {
+                          cudaStream_t st, bool pooled = false, const std::string& tag = "") {
   // wire words -> staging on device -> packed
   const size_t wire_words = n * words_per_point;
-  d_out = static_cast<uint32_t*>(dmalloc(wire_words / 2 * 4));
-  uint32_t* stage = ctx.ws.get_t<uint32_t>("upload.stage", wire_words);
+  d_out = static_cast<uint32_t*>(key_alloc(ctx, pooled, tag, wire_words / 2 * 4));
+  uint32_t* stage = ctx.ws.get_t<uint32_t>(pooled ? "oneshot.stage." + tag : "upload.stage", wire_words);
   h2d(ctx, 0, stage, src, wire_words * 4, st);
   wire_to_packed(st, stage, d_out, wire_words / 16, ctx.d_status);
 }
 
-static void upload_csr(Ctx& ctx, const void* src, uint32_t nc, CsrDev& out, cudaStream_t st) {
+static void upload_csr(Ctx& ctx, const void* src, uint32_t nc, CsrDev& out, cudaStream_t st, bool pooled = false,
+                       const std::string& tag = "") {
   const uint32_t* w = words(src);
   out.nnz = w[0];
-  out.offs = static_cast<uint32_t*>(dmalloc(((size_t)nc + 1) * 4));
-  out.cols = static_cast<uint32_t*>(dmalloc((size_t)out.nnz * 4));
-  out.coeffs = static_cast<uint32_t*>(dmalloc((size_t)out.nnz * 32));
+  out.offs = static_cast<uint32_t*>(key_alloc(ctx, pooled, tag + ".offs", ((size_t)nc + 1) * 4));
+  out.cols = static_cast<uint32_t*>(key_alloc(ctx, pooled, tag + ".cols", (size_t)out.nnz * 4));
+  out.coeffs = static_cast<uint32_t*>(key_alloc(ctx, pooled, tag + ".coeffs", (size_t)out.nnz * 32));
   h2d(ctx, 0, out.offs, w + 1, ((size_t)nc + 1) * 4, st);
   if (out.nnz) {
     uint32_t* stage = ctx.ws.get_t<uint32_t>("upload.csr", 17ull * out.nnz);
@@ -278,8 +286,58 @@ PkDev* pk_upload(Ctx& ctx, const bg_inputs& in, bool build_tables) {
   return pk;
 }
 
+PkDev* pk_stage_oneshot(Ctx& ctx, const bg_inputs& in) {
+  const Header h = parse_header(in);
+  validate_inputs(in, h, false);
+  PkDev* pk = new PkDev();
+  pk->h = h;
+  pk->pooled = true;
+  try {
+    cudaStream_t st = ctx.stream;
+    upload_csr(ctx, in.r1cs_a, h.nc, pk->ca, st, true, "ca");
+    upload_csr(ctx, in.r1cs_b, h.nc, pk->cb, st, true, "cb");
+    upload_csr(ctx, in.r1cs_c, h.nc, pk->cc, st, true, "cc");
+    const uint32_t* g1 = words(in.pk_g1);
+    const uint32_t* g2 = words(in.pk_g2);
+    pk->alpha = host_affine_from_wire<FqOps>(g1);
+    pk->beta = host_affine_from_wire<FqOps>(g1 + 32);
+    pk->delta = host_affine_from_wire<FqOps>(g1 + 64);
+    pk->beta2 = host_affine_from_wire<Fq2Ops>(g2);
+    pk->delta2 = host_affine_from_wire<Fq2Ops>(g2 + 64);
+    // the query sets in the order the proof's accumulations use them (a, b1, b2, l, h), each
+    // with its own staging buffer so no transfer waits for an earlier repack
+    cudaStream_t cs = ctx.copy;
+    BG_CUDA(cudaEventRecord(ctx.event("oneshot.csr"), st));
+    BG_CUDA(cudaStreamWaitEvent(cs, ctx.event("oneshot.csr"), 0));
+    struct Set {
+      int idx;
+      const void* src;
+      size_t n;
+      int words;
+      uint32_t** dst;
+      const char* tag;
+    };
+    const Set sets[5] = {{0, in.pk_a, h.na, 32, &pk->pa, "pa"}, {1, in.pk_b1, h.nb, 32, &pk->pb1, "pb1"},
+                         {2, in.pk_b2, h.nb, 64, &pk->pb2, "pb2"}, {4, in.pk_l, h.nl, 32, &pk->pl, "pl"},
+                         {3, in.pk_h, h.nh, 32, &pk->ph, "ph"}};
+    for (const Set& q : sets) {
+      upload_points(ctx, q.src, q.n, q.words, *q.dst, cs, true, q.tag);
+      pk->ready[q.idx] = ctx.event(std::string("oneshot.ready.") + q.tag);
+      BG_CUDA(cudaEventRecord(pk->ready[q.idx], cs));
+    }
+  } catch (...) {
+    pk_free(pk);
+    throw;
+  }
+  return pk;
+}
+
 void pk_free(PkDev* pk) {
   if (!pk) return;
+  if (pk->pooled) {  // workspace buffers and context events stay with the context
+    delete pk;
+    return;
+  }
   for (uint32_t* p : {pk->pa, pk->pb1, pk->pb2, pk->ph, pk->pl, pk->ca.offs, pk->ca.cols, pk->ca.coeffs,
                       pk->cb.offs, pk->cb.cols, pk->cb.coeffs, pk->cc.offs, pk->cc.cols, pk->cc.coeffs})
     if (p) cudaFree(p);
@@ -424,6 +482,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     cudaStream_t red = ctx.side[1 + j];
     MsmPlan& p = plan[jb.idx];
     p.latency_critical = j == 4;  // only msm_h's reduction is not hidden under an accumulation
+    if (pk.ready[jb.idx]) BG_CUDA(cudaStreamWaitEvent(acc_st, pk.ready[jb.idx], 0));
     t_msm[jb.idx].start(acc_st);
     if (jb.g2) {
       msm_accumulate<Fq2>(ctx, acc_st, jb.tag, jb.pts, *so[j], p, red, jb.tab);

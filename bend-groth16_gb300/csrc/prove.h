@@ -28,6 +28,10 @@ struct PkDev {
   // window tables of the five query sets (a, b1, b2, h, l), built for resident keys
   MsmTable tab[5];
   bool tables = false;
+  // one-shot keys (pk_stage_oneshot): buffers borrowed from the context's workspace, and the
+  // points of each query set (a, b1, b2, h, l) still arriving on the copy stream until ready[i]
+  bool pooled = false;
+  cudaEvent_t ready[5] = {};
 };
 
 Header parse_header(const bg_inputs& in);
@@ -35,6 +39,10 @@ void validate_inputs(const bg_inputs& in, const Header& h, bool need_witness);
 // with build_tables, each query set also gets its 2^(c w) window table (resident keys proving
 // many proofs; a one-shot proof skips them)
 PkDev* pk_upload(Ctx& ctx, const bg_inputs& in, bool build_tables);
+// key of a single proof: CSR and constants uploaded before it returns; the query sets are
+// enqueued on the context's copy stream (ready events in the key) so that the proof's
+// evaluations and QAP overlap their transfer; buffers come from the context's workspace
+PkDev* pk_stage_oneshot(Ctx& ctx, const bg_inputs& in);
 void pk_free(PkDev* pk);
 void check_status(Ctx& ctx, cudaStream_t st);
 void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32_t* rs16, bg_proof* out,
