@@ -7,9 +7,11 @@
 // with g = 5 (bend2/gen/ref_qap.py:59-72).  The reference runs log2(d) Stockham stages on a
 // chunk tree with running-product twiddles (ntt.bend:1-18).
 //
-// Here a transform is a few passes over HBM/L2; each pass loads a tile of up to 2048
+// Here a transform is a few passes over HBM/L2; each pass loads a tile of up to 1024
 // elements into shared memory (limb-major, so a warp's 32 butterflies hit 32 banks), runs up
-// to 11 radix-2 stages there with twiddles from a resident table, and writes the tile back.
+// to 10 radix-2 stages there with twiddles from a resident table, and writes the tile back.
+// 1024-element tiles (32 KiB) give a 2^19 transform 512 CTAs instead of 256 with 64 KiB
+// tiles: measured 2^19 0.219 -> 0.210 ms, 2^20 0.407 -> 0.360 ms.
 //   DIF (Gentleman-Sande): natural order in -> bit-reversed out (used for inverse transforms)
 //   DIT (Cooley-Tukey):    bit-reversed in -> natural order out (forward transforms)
 // so iNTT followed by a coset NTT needs no permutation: the coset factor g^j of coefficient j
@@ -23,9 +25,9 @@
 namespace bg {
 
 constexpr int kNttThreads = 256;
-constexpr int kNttTile = 2048;   // elements per CTA tile (64 KiB of shared memory)
-constexpr int kContigMax = 11;   // stages in the contiguous pass
-constexpr int kStridedMax = 9;   // stages in a strided pass (>= 4 groups of 2^k per tile)
+constexpr int kNttTile = 1024;   // elements per CTA tile (32 KiB of shared memory)
+constexpr int kContigMax = 10;   // stages in the contiguous pass
+constexpr int kStridedMax = 10;  // stages in a strided pass (each element is a whole 32-byte sector)
 
 enum ScaleMode { SC_NONE = 0, SC_NATURAL = 1, SC_BITREV = 2, SC_CONST = 3 };
 
