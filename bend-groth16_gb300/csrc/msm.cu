@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(128) k_bucket_heavy(const uint32_t* __restrict
   }
 }
 constexpr uint32_t kHeavyThreads = 128;
-constexpr uint32_t kHeavyGrid = 32;  // few CTAs: the pass usually finds nothing and should not wait long for SM slots
+constexpr uint32_t kHeavyGrid = 152;
 
 // acc += value of bucket `key` (entries [offsets[key], offsets[key+1])): nothing when empty, the
 // stored bucket when it lies in one slice or is heavy, else its pieces.
