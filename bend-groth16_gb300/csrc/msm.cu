@@ -26,6 +26,7 @@
 #include "msm.h"
 #include "msm_tune.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(128) k_build_table(const uint32_t* __restrict_
 // and its mostly idle lanes.  A bucket of more than kPieceLimit + 1 pieces (a scalar value
 // repeated thousands of times) is joined beforehand by k_bucket_heavy: the thread that owns its
 // first piece lists it in heavy[1 + i] (heavy[0] counts, cleared before the accumulation).
-constexpr uint32_t kPieceLimit = 8;
+constexpr uint32_t kPieceLimit = 24;
 
 template <class F>
 __global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__ points,
@@ -316,24 +317,41 @@ BG_DEV XYZZ<F> add_bucket(XYZZ<F> acc, const uint32_t* __restrict__ offsets, con
   return acc;
 }
 
-// entries per accumulation thread
-template <class F>
-constexpr uint32_t kSlice = 32;
+// Entries per accumulation thread, from a latency model with constants measured on GB300 (G1;
+// G2 scales them alike): a thread's K mixed additions take K x 6.6 us at low occupancy, the
+// whole accumulation cannot beat its throughput (4.58 entries per ns), and a bucket of e
+// entries leaves about e / K + 1 pieces for the reduction (4.5 us each: a 9 us addition, of
+// which half is hidden under other work, fitted to SquareChain(2^12..2^16) proofs).  Large MSMs
+// get 32-entry slices (throughput-bound, fewest pieces); small ones 8 (SquareChain(2^12) proof
+// 2.06 -> 1.69 ms, 2^14 2.44 -> 2.34 ms).
+inline uint32_t slice_entries(size_t max_entries, size_t nkeys) {
+  const double e = (double)max_entries / (double)(nkeys ? nkeys : 1);
+  const double floor_us = (double)max_entries / 4580.0;
+  uint32_t best = 32;
+  double best_us = 1e300;
+  for (uint32_t k = 4; k <= 32; k <<= 1) {
+    const double t = std::max(k * 6.6, floor_us) + (e / k + 2.0) * 4.5;
+    if (t < best_us - 1e-9 || (t <= best_us + 1e-9 && k > best)) {
+      best_us = t;
+      best = k;
+    }
+  }
+  return best;
+}
 
 // Scratch of the bucket phase for at most max_entries entries (words): pieces and the heavy list.
 struct BucketScratch {
+  uint32_t K = 32;            // entries per accumulation thread
   uint32_t* parts = nullptr;  // 2 x slices XYZZ points
   uint32_t* heavy = nullptr;  // 1 + slices / kPieceLimit + 1
 };
-template <class F>
-inline size_t bucket_slices(size_t max_entries) {
-  return (max_entries + kSlice<F> - 1) / kSlice<F>;
-}
+inline size_t bucket_slices(size_t max_entries, uint32_t K) { return (max_entries + K - 1) / K; }
 template <class F, class Get>
-BucketScratch bucket_scratch(size_t max_entries, Get get) {
+BucketScratch bucket_scratch(size_t max_entries, size_t nkeys, Get get, uint32_t K = 0) {
   constexpr int PW = 4 * FieldWords<F>::value;
-  const size_t s = bucket_slices<F>(max_entries);
   BucketScratch b;
+  b.K = K ? K : slice_entries(max_entries, nkeys);
+  const size_t s = bucket_slices(max_entries, b.K);
   b.parts = get("parts", 2 * s * PW);
   b.heavy = get("heavy", s / kPieceLimit + 2);
   return b;
@@ -345,11 +363,11 @@ void bucket_accumulate(Ctx* prof, cudaStream_t st, const uint32_t* points, const
                        const uint32_t* sorted, uint32_t nkeys, size_t max_entries, uint32_t* buckets,
                        const BucketScratch& s) {
   constexpr int FW = FieldWords<F>::value;
-  const size_t slices = bucket_slices<F>(max_entries);
+  const size_t slices = bucket_slices(max_entries, s.K);
   BG_CUDA(cudaMemsetAsync(s.heavy, 0, sizeof(uint32_t), st));
   std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st)
                                        : nullptr);
-  k_bucket_acc<F><<<ceil_div(slices, 128), 128, 0, st>>>(points, offsets, sorted, nkeys, kSlice<F>, buckets, s.parts,
+  k_bucket_acc<F><<<ceil_div(slices, 128), 128, 0, st>>>(points, offsets, sorted, nkeys, s.K, buckets, s.parts,
                                                          s.heavy);
   BG_CHECK_LAUNCH();
 }
@@ -362,7 +380,7 @@ void bucket_heavy(Ctx* prof, cudaStream_t st, const uint32_t* offsets, uint32_t*
   std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_heavy_g1" : "msm_heavy_g2", st)
                                        : nullptr);
   k_bucket_heavy<F><<<kHeavyGrid, kHeavyThreads, kHeavyThreads * PW * sizeof(uint32_t), st>>>(
-      offsets, s.parts, kSlice<F>, s.heavy, buckets);
+      offsets, s.parts, s.K, s.heavy, buckets);
   BG_CHECK_LAUNCH();
 }
 
@@ -445,9 +463,9 @@ int reduce_blocks_per_sm(uint32_t RT) {
   return cache[lrt];
 }
 template <class F>
-ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, int sm_count, uint32_t max_rt) {
+ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, uint32_t K, int sm_count, uint32_t max_rt) {
   const double e = (double)entries / ((double)nb * sets);
-  const double per_bucket = 2.0 + e / 32.0;
+  const double per_bucket = 2.0 + e / K;
   ReduceShape best{nb < 32 ? nb : 32, 1, 1};
   best.J = nb / best.RT;
   double best_cost = 1e300;
@@ -563,8 +581,9 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   plan.entries = so.max_entries;
   Workspace& ws = ctx.ws;
   uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", so.nkeys * PW);
-  const BucketScratch bs = bucket_scratch<F>(
-      so.max_entries, [&](const char* name, size_t words) { return ws.get_t<uint32_t>(tag + ".slice_" + name, words); });
+  const BucketScratch bs = bucket_scratch<F>(so.max_entries, so.nkeys, [&](const char* name, size_t words) {
+    return ws.get_t<uint32_t>(tag + ".slice_" + name, words);
+  });
   if (so.done) BG_CUDA(cudaStreamWaitEvent(st, so.done, 0));
   Ctx* prof = (ctx.profile || ctx.timeline) ? &ctx : nullptr;
   bucket_accumulate<F>(prof, st, d_points, so.offsets, so.sorted, (uint32_t)so.nkeys, so.max_entries, buckets, bs);
@@ -584,13 +603,13 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   // CTA of ~210 registers leaves no room for an accumulation CTA on its SM for its whole
   // (latency-bound) life (K = 18 proof: caps 64 / 128 / 256 measured 11.0 / 10.8 / 10.8 ms).
   const ReduceShape rsh =
-      reduce_shape<F>(so.nb, so.sets, so.max_entries, ctx.sm_count, plan.latency_critical ? 256u : 128u);
+      reduce_shape<F>(so.nb, so.sets, so.max_entries, bs.K, ctx.sm_count, plan.latency_critical ? 256u : 128u);
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
   uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)so.sets * J * 2 * PW);
   {
     KernelTimer kt(ctx, FW == 8 ? "msm_reduce_g1" : "msm_reduce_g2", rs);
-    k_window_reduce<F><<<so.sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(so.offsets, buckets, bs.parts,
-                                                                             kSlice<F>, so.nb, M, J, parts);
+    k_window_reduce<F><<<so.sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(so.offsets, buckets, bs.parts, bs.K,
+                                                                             so.nb, M, J, parts);
     BG_CHECK_LAUNCH();
   }
   plan.fetch_stream = rs;
@@ -766,7 +785,7 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   BG_CUDA(cudaGetDevice(&dev));
   BG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   msm_init_kernels();
-  const ReduceShape rsh = reduce_shape<Fq>(nb, W, max_entries, sms, 256u);
+  const ReduceShape rsh = reduce_shape<Fq>(nb, W, max_entries, 32, sms, 256u);
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
   const unsigned tiles = ceil_div(nkeys + 1, kScanTile);
 
@@ -784,7 +803,9 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   uint32_t* tile_offs = carve(tiles);
   uint32_t* sorted = carve(max_entries);
   uint32_t* buckets = carve(nkeys * PW);
-  const BucketScratch bs = bucket_scratch<Fq>(max_entries, [&](const char*, size_t words) { return carve(words); });
+  // 32-entry slices: the fixed array is sized for them
+  const BucketScratch bs =
+      bucket_scratch<Fq>(max_entries, nkeys, [&](const char*, size_t words) { return carve(words); }, 32);
   uint32_t* parts = carve((size_t)W * J * 2 * PW);
   const size_t host_words = (size_t)W * J * 2 * PW;
   if (off > kNoAllocScratchBytes || host_words > kNoAllocHostWords || tiles > (unsigned)kScanTile)
@@ -811,7 +832,7 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
   BG_CHECK_LAUNCH();
   bucket_accumulate<Fq>(nullptr, st, d_points, offsets, sorted, (uint32_t)nkeys, max_entries, buckets, bs);
   bucket_heavy<Fq>(nullptr, st, offsets, buckets, bs);
-  k_window_reduce<Fq><<<W * J, RT, RT * PW * sizeof(uint32_t), st>>>(offsets, buckets, bs.parts, kSlice<Fq>, nb, M, J,
+  k_window_reduce<Fq><<<W * J, RT, RT * PW * sizeof(uint32_t), st>>>(offsets, buckets, bs.parts, bs.K, nb, M, J,
                                                                      parts);
   BG_CHECK_LAUNCH();
   BG_CUDA(cudaMemcpyAsync(g_noalloc_host_parts, parts, host_words * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));

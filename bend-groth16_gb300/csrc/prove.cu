@@ -562,9 +562,11 @@ static size_t msm_footprint(size_t n, bool g2) {
   if (n == 0) return 0;
   const int c = msm_pick_c(n, g2);
   const size_t W = 254 / c + 1, nb = size_t(1) << (c - 1), nkeys = W * nb;
-  const size_t PW = g2 ? 64 : 32, K = 32;
-  const size_t entries = n * W, threads = (entries + K - 1) / K;
-  const size_t RT = nb < 256 ? nb : 256, M = (nb / RT) < 16 ? nb / RT : 16, J = nb / (RT * M);
+  const size_t PW = g2 ? 64 : 32;
+  const size_t entries = n * W;
+  const size_t K = entries >= (size_t(1) << 21) ? 32 : 4;  // shortest slices of the latency regime
+  const size_t threads = (entries + K - 1) / K;
+  const size_t J = nb < 32 ? 1 : nb / 32;  // most parts a reduction shape can have (RT >= 32)
   // counters, offsets, cursors, entry list, buckets, slice pieces + heavy list, window parts,
   // scan sums
   const size_t words = 3 * (nkeys + 1) + entries + nkeys * PW + 2 * threads * PW + threads / 8 + 2 +
