@@ -17,7 +17,8 @@
 //                     buckets of very many pieces)
 //   5. k_window_reduce one CTA per window part: running sums over M buckets per thread, an
 //                     in-CTA suffix scan and tree sum give sum_b (b+1) B_b for the part
-//   6. host: parts -> window sums -> Horner with c doublings per window -> affine.
+//   6. host: parts -> window sums -> Horner (a window's width of doublings per window) ->
+//      affine.  Windows have balanced widths of at most c bits (window_width).
 // Window sums and the final point are exact group elements, so the affine result equals the
 // reference's for the same inputs regardless of bucket order inside a window.
 #include "common.cuh"
@@ -118,15 +119,24 @@ BG_DEV void load_scalar(uint32_t* s, const uint32_t* __restrict__ scalars, size_
   s[4] = b.x; s[5] = b.y; s[6] = b.z; s[7] = b.w;
 }
 
-// signed digit of window w: returns magnitude (0 = no bucket) and updates carry; *neg set
-// when the digit is negative.  Digits lie in [-(2^(c-1) - 1), 2^(c-1)].
-BG_DEV uint32_t signed_digit(const uint32_t* s, int w, int c, uint32_t& carry, bool& negd) {
-  const uint32_t half = 1u << (c - 1);
-  const uint32_t d = window_bits(s, w * c, c) + carry;
+// Window layout: W windows cover bits [0, 255) (254 scalar bits and room for the last carry)
+// with balanced widths -- the first 255 mod W windows one bit wider -- so that no window is
+// much narrower than the others (a narrow top window would pile its entries into a few huge
+// buckets).  W = floor(254 / c) + 1 keeps every width at most c.
+__host__ __device__ inline int window_width(int w, int W) { return 255 / W + (w < 255 % W ? 1 : 0); }
+__host__ __device__ inline int window_offset(int w, int W) { return w * (255 / W) + (w < 255 % W ? w : 255 % W); }
+
+// signed digit of window w of W: returns magnitude (0 = no bucket) and updates carry; *neg set
+// when the digit is negative.  Digits lie in [-(2^(b-1) - 1), 2^(b-1)] for a window of b bits;
+// scalars below 2^254 leave no carry out of the top window.
+BG_DEV uint32_t signed_digit(const uint32_t* s, int w, int W, uint32_t& carry, bool& negd) {
+  const int b = window_width(w, W);
+  const uint32_t half = 1u << (b - 1);
+  const uint32_t d = window_bits(s, window_offset(w, W), b) + carry;
   if (d > half) {
     carry = 1u;
     negd = true;
-    return (1u << c) - d;
+    return (1u << b) - d;
   }
   carry = 0u;
   negd = false;
@@ -135,7 +145,7 @@ BG_DEV uint32_t signed_digit(const uint32_t* s, int w, int c, uint32_t& carry, b
 
 // Bucket key of window w's digit: w * key_stride + |d| - 1 (key_stride = 2^(c-1): one bucket
 // set per window; 0: all windows share one set).  Point index stored with it:
-// i + w * idx_stride (0: the point itself; n: row w of a table of 2^(c w)-multiples).
+// i + w * idx_stride (0: the point itself; n: row w of a table of 2^(o_w)-multiples).
 __global__ void k_digits_hist(const uint32_t* __restrict__ scalars, size_t n, int c, int W, uint32_t key_stride,
                               uint32_t* __restrict__ counts, uint32_t* __restrict__ status) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -149,7 +159,7 @@ __global__ void k_digits_hist(const uint32_t* __restrict__ scalars, size_t n, in
   uint32_t carry = 0;
   for (int w = 0; w < W; w++) {
     bool ng;
-    const uint32_t mag = signed_digit(s, w, c, carry, ng);
+    const uint32_t mag = signed_digit(s, w, W, carry, ng);
     if (mag) atomicAdd(&counts[(size_t)w * key_stride + mag - 1], 1u);
   }
 }
@@ -164,7 +174,7 @@ __global__ void k_scatter(const uint32_t* __restrict__ scalars, size_t n, int c,
   uint32_t carry = 0;
   for (int w = 0; w < W; w++) {
     bool ng;
-    const uint32_t mag = signed_digit(s, w, c, carry, ng);
+    const uint32_t mag = signed_digit(s, w, W, carry, ng);
     if (mag) {
       const uint32_t slot = atomicAdd(&cursor[(size_t)w * key_stride + mag - 1], 1u);
       sorted[slot] = ((uint32_t)i + (uint32_t)w * idx_stride) | (ng ? 0x80000000u : 0u);
@@ -172,9 +182,9 @@ __global__ void k_scatter(const uint32_t* __restrict__ scalars, size_t n, int c,
   }
 }
 
-// Window table of a fixed point set: row w holds 2^(c w) P_i (affine, row-major, n points per
-// row); computed once per proving key, one thread per point (c doublings per row, one
-// inversion per entry).
+// Window table of a fixed point set: row w holds 2^(o_w) P_i, o_w the offset of window w
+// (affine, row-major, n points per row); computed once per proving key, one thread per point
+// (a window's width of doublings per row, one inversion per entry).
 template <class F>
 __global__ void __launch_bounds__(128) k_build_table(const uint32_t* __restrict__ pts, size_t n, int c, int W,
                                                      uint32_t* __restrict__ table) {
@@ -185,7 +195,7 @@ __global__ void __launch_bounds__(128) k_build_table(const uint32_t* __restrict_
   store_affine(table + i * PW, p);
   XYZZ<F> q = xyzz_from_affine(p);
   for (int w = 1; w < W; w++) {
-    for (int d = 0; d < c; d++) q = xyzz_dbl(q);
+    for (int d = 0; d < window_width(w - 1, W); d++) q = xyzz_dbl(q);
     Affine<F> a;
     if (is_inf(q)) {
       a.x = field_zero<F>();
@@ -673,14 +683,14 @@ void msm_fetch(Ctx& ctx, cudaStream_t st, MsmPlan& plan) {
   ctx.d2h_bytes += (uint64_t)plan.W * plan.J * 2 * PW * sizeof(uint32_t);
 }
 
-// Window w = sum_j S_j + span * sum_j j R_j; total = sum_w 2^(c w) window_w (Horner).
+// Window w = sum_j S_j + span * sum_j j R_j; total = sum_w 2^(o_w) window_w (Horner).
 template <class F>
 void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32) {
   typedef typename HostField<F>::T H;
   constexpr int PW = 4 * H::WORDS;
   bgh::Xyzz<H> acc = bgh::xyzz_inf<H>();
   for (int w = plan.W - 1; w >= 0; w--) {
-    for (int d = 0; d < plan.c; d++) acc = bgh::xyzz_dbl(acc);
+    for (int d = 0; d < window_width(w, plan.W); d++) acc = bgh::xyzz_dbl(acc);
     const uint32_t* pw = plan.host_window_sums + (size_t)w * plan.J * 2 * PW;
     bgh::Xyzz<H> s = bgh::xyzz_inf<H>(), run = bgh::xyzz_inf<H>(), jr = bgh::xyzz_inf<H>();
     for (int j = (int)plan.J - 1; j >= 0; j--) {

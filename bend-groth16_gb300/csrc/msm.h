@@ -24,7 +24,8 @@ struct MsmPlan {
   bool latency_critical = true;
 };
 
-// Window table of a fixed point set: row w (w < W) holds 2^(c w) P_i for all i, so every
+// Window table of a fixed point set: row w (w < W) holds 2^(o_w) P_i for all i (o_w the bit
+// offset of window w in the balanced layout of msm.cu), so every
 // window's digits index one shared bucket set (no window combination afterwards).
 struct MsmTable {
   uint32_t* d = nullptr;  // W rows of n packed affine points (device, owned by the key)
