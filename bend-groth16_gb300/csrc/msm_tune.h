@@ -9,11 +9,11 @@ constexpr int kTuneMinLog2 = 10;
 constexpr int kTuneMaxLog2 = 22;
 // one bucket set per window (standalone MSMs, one-shot proofs)
 constexpr signed char kTuneSets[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
-    {5, 8, 8, 8, 9, 10, 13, 15, 15, 15, 15, 15, 17},
-    {5, 8, 8, 8, 9, 10, 13, 12, 13, 15, 15, 0, 0}};
+    {8, 8, 9, 9, 9, 10, 11, 12, 15, 15, 15, 15, 17},
+    {8, 9, 9, 9, 9, 10, 11, 12, 15, 15, 15, 0, 0}};
 // window tables of resident keys (one shared bucket set)
 constexpr signed char kTuneTables[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
     {9, 0, 11, 0, 13, 0, 15, 0, 17, 0, 19, 0, 0},
-    {10, 0, 12, 0, 13, 0, 15, 0, 17, 0, 19, 0, 0}};
+    {10, 0, 11, 0, 14, 0, 15, 0, 17, 0, 17, 0, 0}};
 
 }  // namespace bg

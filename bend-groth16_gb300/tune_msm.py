@@ -5,11 +5,11 @@ on the GPU it runs on and writes the table the library compiles in (csrc/msm_tun
 
 Two layouts are tuned, as the library uses them:
   * one bucket set per window (bg_msm_g1/g2, one-shot proofs): the standalone MSM over n
-    points for c in [rule - 2, rule + 2];
+    points for c in [rule - 2, rule + 2], widened while the fastest c is on an edge;
   * window tables of resident keys (one shared bucket set): whole SquareChain(2^K) proofs
-    against a key uploaded with the table width of one curve forced to c in [rule - 1, rule + 1]
-    (every G1 query of that proof has floor(log2 n) = K, and so does the G2 one), G1 first, then
-    G2 with G1 at its best.
+    against a key uploaded with the table width of one curve forced to c in [rule - 1, rule + 1],
+    widened the same way (every G1 query of that proof has floor(log2 n) = K, and so does the
+    G2 one), G1 first, then G2 with G1 at its best.
 Timings are medians of wall-clock calls of the synchronous API (device work included).  Sizes
 the run skips keep 0 in the table (the library's size rule applies there).
 """
@@ -39,6 +39,23 @@ def median_ms(fn, reps):
     return statistics.median(out)
 
 
+def search(measure, lo, hi, c_min, c_max):
+    """times of c in [lo, hi] (clamped to [c_min, c_max]), the range widened one step at a time
+    while the fastest width sits on an edge of it"""
+    lo, hi = max(c_min, lo), min(c_max, hi)
+    times = {c: measure(c) for c in range(lo, hi + 1)}
+    while True:
+        best = min(times, key=times.get)
+        if best == lo and lo > c_min:
+            lo -= 1
+            times[lo] = measure(lo)
+        elif best == hi and hi < c_max:
+            hi += 1
+            times[hi] = measure(hi)
+        else:
+            return times
+
+
 def tune_sets(ctx, torch, pts_g1, pts_g2, log2s_g1, log2s_g2, reps, log):
     """layout 0: standalone MSMs over device-resident points and uniform scalars below r"""
     dev = torch.device("cuda")
@@ -54,11 +71,12 @@ def tune_sets(ctx, torch, pts_g1, pts_g2, log2s_g1, log2s_g2, reps, log):
             reps_needed = (n * pw + pts.numel() - 1) // pts.numel()
             p = pts.repeat(reps_needed)[: n * pw].contiguous()
             rule = bendg.lib().bg_msm_window_bits(n, curve)
-            times = {}
-            for c in range(max(3, rule - 2), min(20, rule + 2) + 1):
+            f = ctx.msm_g1_dev if curve == bendg.CURVE_G1 else ctx.msm_g2_dev
+
+            def measure(c):
                 ctx.window_override(0, curve, c)
-                f = ctx.msm_g1_dev if curve == bendg.CURVE_G1 else ctx.msm_g2_dev
-                times[c] = median_ms(lambda: f(p.data_ptr(), sc.data_ptr(), n), reps)
+                return median_ms(lambda: f(p.data_ptr(), sc.data_ptr(), n), reps)
+            times = search(measure, rule - 2, rule + 2, 3, 20)
             ctx.window_override(0, curve, 0)
             c_best = min(times, key=times.get)
             best[curve][lg] = c_best
@@ -81,13 +99,15 @@ def tune_tables(ctx, ks, data_root, reps, log):
         for curve in (bendg.CURVE_G1, bendg.CURVE_G2):
             n = int(hdr[4]) if curve == bendg.CURVE_G1 else int(hdr[5])
             rule = bendg.lib().bg_msm_table_window_bits(n, curve)
-            times = {}
-            for c in range(max(6, rule - 1), min(20, rule + 1) + 1):
+
+            def measure(c):
                 for cv in (0, 1):
                     ctx.window_override(1, cv, forced[cv] if cv != curve else c)
                 key = ctx.pk_upload(files)
-                times[c] = median_ms(lambda: key.prove(w, rs), reps)
+                t = median_ms(lambda: key.prove(w, rs), reps)
                 key.release()
+                return t
+            times = search(measure, rule - 1, rule + 1, 6, 20)
             c_best = min(times, key=times.get)
             forced[curve] = c_best
             best[curve][k] = c_best

@@ -1,0 +1,56 @@
+"""Host logic of the window-width autotuner (bend-groth16_gb300/tune_msm.py): the search that
+widens its range while the fastest width sits on an edge, and the header it writes, which the
+library compiles in.  No GPU: the measurements are a fake cost curve."""
+import re
+
+import tune_msm
+
+
+def test_search_widens_past_the_lower_edge():
+    calls = []
+
+    def cost(c):
+        calls.append(c)
+        return abs(c - 7) + 1.0
+    times = tune_msm.search(cost, 10, 14, 3, 20)
+    assert min(times, key=times.get) == 7
+    assert sorted(times) == list(range(6, 15))      # one width past the optimum, then stop
+    assert len(calls) == len(set(calls))            # nothing measured twice
+
+
+def test_search_widens_past_the_upper_edge_and_clamps():
+    times = tune_msm.search(lambda c: -c, 16, 19, 3, 20)
+    assert sorted(times) == [16, 17, 18, 19, 20]    # stops at c_max
+    times = tune_msm.search(lambda c: c, 1, 5, 3, 20)
+    assert sorted(times) == [3, 4, 5]               # clamped below, optimum on c_min
+
+
+def test_search_interior_optimum_measures_only_the_range():
+    times = tune_msm.search(lambda c: (c - 12) ** 2, 10, 14, 3, 20)
+    assert sorted(times) == [10, 11, 12, 13, 14]
+
+
+def test_header_text_rows():
+    sets = {0: {10: 8, 11: 9, 22: 17}, 1: {10: 8}}
+    tables = {0: {18: 17}, 1: {}}
+    h = tune_msm.header_text(sets, tables, "test gpu")
+    rows = re.findall(r"\{([0-9, ]+)\}", h)
+    assert len(rows) == 4
+    vals = [[int(x) for x in r.split(",")] for r in rows]
+    assert all(len(v) == tune_msm.MAX_LOG2 - tune_msm.MIN_LOG2 + 1 for v in vals)
+    assert vals[0][0] == 8 and vals[0][1] == 9 and vals[0][-1] == 17 and vals[0][5] == 0
+    assert vals[1][0] == 8 and sum(vals[1]) == 8
+    assert vals[2][18 - tune_msm.MIN_LOG2] == 17 and sum(vals[3]) == 0
+    assert "kTuneMinLog2 = %d" % tune_msm.MIN_LOG2 in h
+
+
+def test_committed_header_is_in_range():
+    """the committed table holds 0 (size rule) or a width the MSM supports, per curve and size"""
+    import os
+    src = open(os.path.join(os.path.dirname(tune_msm.__file__), "csrc", "msm_tune.h")).read()
+    rows = re.findall(r"\{([0-9, ]+)\}", src)
+    assert len(rows) == 4
+    for r in rows:
+        v = [int(x) for x in r.split(",")]
+        assert len(v) == tune_msm.MAX_LOG2 - tune_msm.MIN_LOG2 + 1
+        assert all(x == 0 or 3 <= x <= 20 for x in v)
