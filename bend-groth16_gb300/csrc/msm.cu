@@ -224,9 +224,12 @@ __global__ void __launch_bounds__(128) k_build_table(const uint32_t* __restrict_
 // repeated thousands of times) is joined beforehand by k_bucket_heavy: the thread that owns its
 // first piece lists it in heavy[1 + i] (heavy[0] counts, cleared before the accumulation).
 constexpr uint32_t kPieceLimit = 24;
+// CTA size of the accumulation
+template <class F>
+constexpr int kAccThreads = 128;
 
 template <class F>
-__global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* __restrict__ points,
+__global__ void __launch_bounds__(kAccThreads<F>) k_bucket_acc(const uint32_t* __restrict__ points,
                                                     const uint32_t* __restrict__ offsets,
                                                     const uint32_t* __restrict__ sorted, uint32_t nbuckets,
                                                     uint32_t K, uint32_t* __restrict__ buckets,
@@ -356,11 +359,41 @@ struct BucketScratch {
   uint32_t* heavy = nullptr;  // 1 + slices / kPieceLimit + 1
 };
 inline size_t bucket_slices(size_t max_entries, uint32_t K) { return (max_entries + K - 1) / K; }
+
+// Accumulation threads resident on the whole GPU at once (SMs x CTAs per SM x CTA size).
+template <class F>
+double acc_slots() {
+  static double slots = 0;
+  if (slots == 0) {
+    int dev = 0, sms = 0, occ = 0;
+    BG_CUDA(cudaGetDevice(&dev));
+    BG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    BG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bucket_acc<F>, kAccThreads<F>, 0));
+    slots = (double)sms * (occ > 0 ? occ : 1) * kAccThreads<F>;
+  }
+  return slots;
+}
+
+// Every slice costs the same K additions, so an accumulation grid of 1.6 waves takes as long
+// as 2.  When the model's slices need more than one wave, K is rounded so that the grid is a
+// whole number of waves (the nearest, at least one): SquareChain(2^18) proof 11.05 -> 10.7 ms,
+// G2 accumulation 2^18 3.25 -> 2.95 ms.  Slices then hold at least 3/4 of the model's K
+// (rounding 1.5 waves up to 2 at worst); the model picks K = 32 for every MSM that needs more
+// than a wave and at least 2^21 entries.
+template <class F>
+uint32_t whole_wave_slices(size_t max_entries, uint32_t K) {
+  const double slots = acc_slots<F>();
+  const double waves = std::ceil((double)max_entries / K) / slots;
+  if (waves <= 1.0) return K;
+  const double rounded = std::max(1.0, std::round(waves));
+  return (uint32_t)std::ceil((double)max_entries / (rounded * slots));
+}
+
 template <class F, class Get>
 BucketScratch bucket_scratch(size_t max_entries, size_t nkeys, Get get, uint32_t K = 0) {
   constexpr int PW = 4 * FieldWords<F>::value;
   BucketScratch b;
-  b.K = K ? K : slice_entries(max_entries, nkeys);
+  b.K = K ? K : whole_wave_slices<F>(max_entries, slice_entries(max_entries, nkeys));
   const size_t s = bucket_slices(max_entries, b.K);
   b.parts = get("parts", 2 * s * PW);
   b.heavy = get("heavy", s / kPieceLimit + 2);
@@ -377,7 +410,7 @@ void bucket_accumulate(Ctx* prof, cudaStream_t st, const uint32_t* points, const
   BG_CUDA(cudaMemsetAsync(s.heavy, 0, sizeof(uint32_t), st));
   std::unique_ptr<KernelTimer> kt(prof ? new KernelTimer(*prof, FW == 8 ? "msm_bucket_acc_g1" : "msm_bucket_acc_g2", st)
                                        : nullptr);
-  k_bucket_acc<F><<<ceil_div(slices, 128), 128, 0, st>>>(points, offsets, sorted, nkeys, s.K, buckets, s.parts,
+  k_bucket_acc<F><<<ceil_div(slices, kAccThreads<F>), kAccThreads<F>, 0, st>>>(points, offsets, sorted, nkeys, s.K, buckets, s.parts,
                                                          s.heavy);
   BG_CHECK_LAUNCH();
 }

@@ -564,7 +564,8 @@ static size_t msm_footprint(size_t n, bool g2) {
   const size_t W = 254 / c + 1, nb = size_t(1) << (c - 1), nkeys = W * nb;
   const size_t PW = g2 ? 64 : 32;
   const size_t entries = n * W;
-  const size_t K = entries >= (size_t(1) << 21) ? 32 : 4;  // shortest slices of the latency regime
+  // shortest slices: 3/4 of 32 after whole-wave rounding, 4 in the latency regime
+  const size_t K = entries >= (size_t(1) << 21) ? 24 : 4;
   const size_t threads = (entries + K - 1) / K;
   const size_t J = nb < 32 ? 1 : nb / 32;  // most parts a reduction shape can have (RT >= 32)
   // counters, offsets, cursors, entry list, buckets, slice pieces + heavy list, window parts,
