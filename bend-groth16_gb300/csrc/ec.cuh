@@ -157,7 +157,9 @@ BG_DEV XYZZ<F> xyzz_madd(const XYZZ<F>& p, const Affine<F>& q) {
   return r;
 }
 
-// P + Q for XYZZ P, Q (add-2008-s)
+// P + Q for XYZZ P, Q (add-2008-s).  The products that read p and q come first, so neither
+// input is live past them: (u1, s1, zz1 zz2, zzz1 zzz2) is p itself in other coordinates
+// (x = u1 / (zz1 zz2), y = s1 / (zzz1 zzz2)), and the P = Q case doubles that.
 template <class F>
 BG_DEV XYZZ<F> xyzz_add(const XYZZ<F>& p, const XYZZ<F>& q) {
   if (is_inf(q)) return p;
@@ -166,10 +168,12 @@ BG_DEV XYZZ<F> xyzz_add(const XYZZ<F>& p, const XYZZ<F>& q) {
   const F u2 = fmul(q.x, p.zz);
   const F s1 = fmul(p.y, q.zzz);
   const F s2 = fmul(q.y, p.zzz);
+  const F zz12 = fmul(p.zz, q.zz);
+  const F zzz12 = fmul(p.zzz, q.zzz);
   const F pp_ = sub(u2, u1);
   const F r_ = sub(s2, s1);
   if (is_zero(pp_)) {
-    if (is_zero(r_)) return xyzz_dbl(p);
+    if (is_zero(r_)) return xyzz_dbl(XYZZ<F>{u1, s1, zz12, zzz12});
     return xyzz_inf<F>();
   }
   const F pp = fsqr(pp_);
@@ -178,8 +182,8 @@ BG_DEV XYZZ<F> xyzz_add(const XYZZ<F>& p, const XYZZ<F>& q) {
   XYZZ<F> r;
   r.x = sub(sub(fsqr(r_), ppp), dbl(qq));
   r.y = fmul_sub(r_, sub(qq, r.x), s1, ppp);
-  r.zz = fmul(fmul(p.zz, q.zz), pp);
-  r.zzz = fmul(fmul(p.zzz, q.zzz), ppp);
+  r.zz = fmul(zz12, pp);
+  r.zzz = fmul(zzz12, ppp);
   return r;
 }
 

@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "ec.cuh"
 #include "host_ff.hpp"
+#include "host_pool.hpp"
 #include "msm.h"
 #include "msm_tune.h"
 
@@ -32,6 +33,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <vector>
 
 namespace bg {
 
@@ -459,8 +461,8 @@ __global__ void k_window_reduce(const uint32_t* __restrict__ offsets, const uint
     store_xyzz(sm + (size_t)t * PW, run);
     __syncthreads();
   }
-  XYZZ<F> total_r;
-  if (t == 0) total_r = run;
+  // R_j, written at once so that it holds no registers through the tree below
+  if (t == 0) store_xyzz(out + ((size_t)blockIdx.x * 2 + 1) * PW, run);
   // Y_t = T_t + M Suf_t (t >= 1), Y_0 = T_0
   if (t >= 1) {
     for (uint32_t m = M; m > 1; m >>= 1) run = xyzz_dbl(run);
@@ -476,10 +478,7 @@ __global__ void k_window_reduce(const uint32_t* __restrict__ offsets, const uint
     }
     __syncthreads();
   }
-  if (t == 0) {
-    store_xyzz(out + (size_t)blockIdx.x * 2 * PW, acc);
-    store_xyzz(out + ((size_t)blockIdx.x * 2 + 1) * PW, total_r);
-  }
+  if (t == 0) store_xyzz(out + (size_t)blockIdx.x * 2 * PW, acc);
 }
 
 // Shape of the window reduction: RT threads x M buckets per thread x J parts per window, picked
@@ -721,9 +720,9 @@ template <class F>
 void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32) {
   typedef typename HostField<F>::T H;
   constexpr int PW = 4 * H::WORDS;
-  bgh::Xyzz<H> acc = bgh::xyzz_inf<H>();
-  for (int w = plan.W - 1; w >= 0; w--) {
-    for (int d = 0; d < window_width(w, plan.W); d++) acc = bgh::xyzz_dbl(acc);
+  // window w's sum from its J parts: sum_j S_j + span sum_{j>=1} j R_j (independent per window)
+  std::vector<bgh::Xyzz<H>> wsum(plan.W);
+  auto window_sum = [&](int w) {
     const uint32_t* pw = plan.host_window_sums + (size_t)w * plan.J * 2 * PW;
     bgh::Xyzz<H> s = bgh::xyzz_inf<H>(), run = bgh::xyzz_inf<H>(), jr = bgh::xyzz_inf<H>();
     for (int j = (int)plan.J - 1; j >= 0; j--) {
@@ -734,7 +733,19 @@ void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32) {
       }
     }
     for (uint32_t m = plan.part_span; m > 1; m >>= 1) jr = bgh::xyzz_dbl(jr);
-    acc = bgh::xyzz_add(acc, bgh::xyzz_add(s, jr));
+    wsum[w] = bgh::xyzz_add(s, jr);
+  };
+  // The window sums of a bucket-set-per-window MSM are about two thirds of its host work
+  // (17 windows x 8 parts: ~550 of ~850 point operations); they run on the host pool, the
+  // Horner chain after them stays serial.  SquareChain(2^18) one-shot proof: the G2 finish is
+  // the tail of the proof.
+  if (plan.W >= 4 && (size_t)plan.W * plan.J >= 32) HostPool::get().parallel_for(plan.W, window_sum);
+  else
+    for (int w = 0; w < plan.W; w++) window_sum(w);
+  bgh::Xyzz<H> acc = bgh::xyzz_inf<H>();
+  for (int w = plan.W - 1; w >= 0; w--) {
+    for (int d = 0; d < window_width(w, plan.W); d++) acc = bgh::xyzz_dbl(acc);
+    acc = bgh::xyzz_add(acc, wsum[w]);
   }
   bgh::aff_to_words32<H>(out_affine_words32, bgh::xyzz_to_affine(acc));
 }

@@ -37,6 +37,16 @@ struct ScaleTab {
   int bits = 0;
 };
 
+// a b as the 512-bit Karatsuba product and one Montgomery reduction (232 multiply-adds instead
+// of CIOS's 264; the inputs are below r, so the product is below r R): 2^20 forward transform
+// 0.357 -> 0.352 ms, bit-identical.  Stage-pair register blocks (radix-4 sets, half the
+// shared-memory round trips) were measured slower, 0.40 ms.
+BG_DEV Fr mul_kara(const Fr& a, const Fr& b) {
+  Wide t;
+  wide_mul(t, a.v, b.v);
+  return redc<FrParams>(t);
+}
+
 BG_DEV Fr scale_factor(int mode, size_t j, int L, const ScaleTab& t) {
   if (mode == SC_CONST) return load_fp<FrParams>(t.hi);
   size_t i = j;
@@ -104,12 +114,12 @@ __global__ void __launch_bounds__(kNttThreads) k_ntt_pass(uint32_t* __restrict__
       } else {
         const Fr w = load_fp<FrParams>(tw + 8 * widx);
         if (DIT) {
-          x2 = mul(x2, w);
+          x2 = mul_kara(x2, w);
           y1 = add(x1, x2);
           y2 = sub(x1, x2);
         } else {
           y1 = add(x1, x2);
-          y2 = mul(sub(x1, x2), w);
+          y2 = mul_kara(sub(x1, x2), w);
         }
       }
 #pragma unroll

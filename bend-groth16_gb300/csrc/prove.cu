@@ -517,18 +517,23 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   // C = s A + r B1 - r s delta + (mL + mH)
   auto g1 = [](const uint32_t* w) { return bgh::xyzz_from(bgh::aff_from_words32<FqOps>(w)); };
   uint32_t res[5][32];
-  BG_CUDA(cudaStreamSynchronize(ctx.side[1]));
+  // an MSM's window parts are on the host once its reduction stream drains (an empty MSM has
+  // no stream: nothing to wait for)
+  auto drain = [](const MsmPlan& p) {
+    if (p.fetch_stream) BG_CUDA(cudaStreamSynchronize(p.fetch_stream));
+  };
+  drain(plan[0]);
   msm_finish<Fq>(plan[0], res[0]);
   const Xyzz<FqOps> A = bgh::xyzz_add(bgh::xyzz_add(g1(res[0]), r_delta), bgh::xyzz_from(pk.alpha));
-  BG_CUDA(cudaStreamSynchronize(ctx.side[2]));
+  drain(plan[1]);
   msm_finish<Fq>(plan[1], res[1]);
   const Xyzz<FqOps> B1 = bgh::xyzz_add(bgh::xyzz_add(g1(res[1]), s_delta), bgh::xyzz_from(pk.beta));
   Xyzz<FqOps> c_part = bgh::xyzz_add(bgh::xyzz_add(bgh::xyzz_mul(A, s), bgh::xyzz_mul(B1, r)), bgh::xyzz_neg(rs_delta));
-  BG_CUDA(cudaStreamSynchronize(ctx.side[3]));
+  drain(plan[2]);
   msm_finish<Fq2>(plan[2], res[2]);
   const Xyzz<Fq2Ops> B2 = bgh::xyzz_add(
       bgh::xyzz_add(bgh::xyzz_from(bgh::aff_from_words32<Fq2Ops>(res[2])), s_delta2), bgh::xyzz_from(pk.beta2));
-  BG_CUDA(cudaStreamSynchronize(ctx.side[4]));
+  drain(plan[4]);
   msm_finish<Fq>(plan[4], res[4]);
   c_part = bgh::xyzz_add(c_part, g1(res[4]));
   for (int j = 0; j < kStreams; j++) BG_CUDA(cudaStreamSynchronize(ctx.side[j]));
