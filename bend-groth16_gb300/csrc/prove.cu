@@ -477,19 +477,29 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   for (int j = 0; j < 4; j++) so[j] = &sort_for(jobs[j], sort_st);
   so[4] = &sort_for(jobs[4], st);  // st: after the QAP
   BG_CUDA(cudaStreamWaitEvent(acc_st, ctx.ev_fork, 0));
+  // A small proof's accumulations together fill less than one wave of the GPU (short slices:
+  // about entries / 8 threads each), so queueing them on one stream would leave it mostly
+  // idle: each MSM then runs its whole chain -- accumulation, heavy pass, reduction -- on its
+  // own stream, and the five overlap.
+  size_t acc_threads = 0;
+  for (int j = 0; j < 5; j++) acc_threads += so[j]->max_entries / 8 + 1;
+  const bool overlap = acc_threads <= (size_t)ctx.sm_count * 4 * 128;
   for (int j = 0; j < 5; j++) {
     const Job& jb = jobs[j];
     cudaStream_t red = ctx.side[1 + j];
+    cudaStream_t ast = overlap ? red : acc_st;
     MsmPlan& p = plan[jb.idx];
-    p.latency_critical = j == 4;  // only msm_h's reduction is not hidden under an accumulation
-    if (pk.ready[jb.idx]) BG_CUDA(cudaStreamWaitEvent(acc_st, pk.ready[jb.idx], 0));
-    t_msm[jb.idx].start(acc_st);
+    // only msm_h's reduction is not hidden under a later accumulation; overlapped, none is
+    p.latency_critical = overlap || j == 4;
+    if (overlap) BG_CUDA(cudaStreamWaitEvent(ast, ctx.ev_fork, 0));
+    if (pk.ready[jb.idx]) BG_CUDA(cudaStreamWaitEvent(ast, pk.ready[jb.idx], 0));
+    t_msm[jb.idx].start(ast);
     if (jb.g2) {
-      msm_accumulate<Fq2>(ctx, acc_st, jb.tag, jb.pts, *so[j], p, red, jb.tab);
-      msm_fetch<Fq2>(ctx, acc_st, p);
+      msm_accumulate<Fq2>(ctx, ast, jb.tag, jb.pts, *so[j], p, red, jb.tab);
+      msm_fetch<Fq2>(ctx, ast, p);
     } else {
-      msm_accumulate<Fq>(ctx, acc_st, jb.tag, jb.pts, *so[j], p, red, jb.tab);
-      msm_fetch<Fq>(ctx, acc_st, p);
+      msm_accumulate<Fq>(ctx, ast, jb.tag, jb.pts, *so[j], p, red, jb.tab);
+      msm_fetch<Fq>(ctx, ast, p);
     }
     t_msm[jb.idx].stop(red);
   }
