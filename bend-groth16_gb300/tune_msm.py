@@ -118,6 +118,17 @@ def tune_tables(ctx, ks, data_root, reps, log):
     return best
 
 
+def committed_tables(path):
+    """the kTuneSets / kTuneTables rows of an existing header, as {curve: {log2 n: c}} (nonzero only)"""
+    import re
+    rows = re.findall(r"\{([0-9, ]+)\}", open(path).read())
+    out = []
+    for r in rows[:4]:
+        vals = [int(x) for x in r.split(",")]
+        out.append({MIN_LOG2 + i: v for i, v in enumerate(vals) if v})
+    return {0: out[0], 1: out[1]}, {0: out[2], 1: out[3]}
+
+
 def header_text(sets, tables, gpu):
     def row(d):
         return "{" + ", ".join(str(d.get(lg, 0)) for lg in range(MIN_LOG2, MAX_LOG2 + 1)) + "}"
@@ -150,6 +161,8 @@ def main():
     ap.add_argument("--data-root", default="/tmp/bg_tune")
     ap.add_argument("--max-sets-log2", type=int, default=22)
     ap.add_argument("--table-ks", default="10,12,14,16,18,20")
+    ap.add_argument("--keep", default=None,
+                    help="an existing msm_tune.h whose entries are kept where this run measures nothing")
     args = ap.parse_args()
     import torch
     ctx = bendg.Context(0)
@@ -159,28 +172,37 @@ def main():
         print(s, flush=True)
         log_lines.append(s)
 
-    # base points: the h and b2 queries of a SquareChain(2^20) instance, tiled as needed
-    base = os.path.join(args.data_root, "sq20")
-    if not os.path.exists(os.path.join(base, "vk.bin")):
-        ctx.synth_square_chain(20, 4262, base)
-    files = bendg.HostFiles(base)
-    dev = torch.device("cuda")
+    sets = {0: {}, 1: {}}
+    if args.max_sets_log2 >= MIN_LOG2:
+        # base points: the h and b2 queries of a SquareChain(2^20) instance, tiled as needed
+        base = os.path.join(args.data_root, "sq20")
+        if not os.path.exists(os.path.join(base, "vk.bin")):
+            ctx.synth_square_chain(20, 4262, base)
+        files = bendg.HostFiles(base)
+        dev = torch.device("cuda")
 
-    def packed(name, count):
-        words = files.words(name)
-        n = words.size // (32 if name != "pk_b2" else 64)
-        n = min(n, count)
-        wire = torch.from_numpy(words[: n * (32 if name != "pk_b2" else 64)].astype(np.int64).astype(np.int32)).to(dev)
-        out = torch.empty(wire.numel() // 2, dtype=torch.int32, device=dev)
-        ctx.repack_to_packed_dev(wire.data_ptr(), out.data_ptr(), wire.numel() // 16)
-        torch.cuda.synchronize()
-        return out
+        def packed(name, count):
+            words = files.words(name)
+            n = words.size // (32 if name != "pk_b2" else 64)
+            n = min(n, count)
+            wire = torch.from_numpy(words[: n * (32 if name != "pk_b2" else 64)].astype(np.int64).astype(np.int32))
+            wire = wire.to(dev)
+            out = torch.empty(wire.numel() // 2, dtype=torch.int32, device=dev)
+            ctx.repack_to_packed_dev(wire.data_ptr(), out.data_ptr(), wire.numel() // 16)
+            torch.cuda.synchronize()
+            return out
 
-    pts_g1 = packed("pk_h", 1 << 21)
-    pts_g2 = packed("pk_b2", 1 << 20)
-    sets = tune_sets(ctx, torch, pts_g1, pts_g2, range(MIN_LOG2, args.max_sets_log2 + 1),
-                     range(MIN_LOG2, min(args.max_sets_log2, 20) + 1), args.reps, log)
-    tables = tune_tables(ctx, [int(k) for k in args.table_ks.split(",")], args.data_root, args.reps, log)
+        pts_g1 = packed("pk_h", 1 << 21)
+        pts_g2 = packed("pk_b2", 1 << 20)
+        sets = tune_sets(ctx, torch, pts_g1, pts_g2, range(MIN_LOG2, args.max_sets_log2 + 1),
+                         range(MIN_LOG2, min(args.max_sets_log2, 20) + 1), args.reps, log)
+    tables = tune_tables(ctx, [int(k) for k in args.table_ks.split(",") if k], args.data_root, args.reps, log)
+    if args.keep:
+        old_sets, old_tables = committed_tables(args.keep)
+        for new, old in ((sets, old_sets), (tables, old_tables)):
+            for curve in (0, 1):
+                for lg, c in old[curve].items():
+                    new[curve].setdefault(lg, c)
     gpu = torch.cuda.get_device_name(0)
     with open(args.out, "w") as f:
         f.write(header_text(sets, tables, gpu))

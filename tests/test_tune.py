@@ -54,3 +54,12 @@ def test_committed_header_is_in_range():
         v = [int(x) for x in r.split(",")]
         assert len(v) == tune_msm.MAX_LOG2 - tune_msm.MIN_LOG2 + 1
         assert all(x == 0 or 3 <= x <= 20 for x in v)
+
+
+def test_committed_tables_round_trip(tmp_path):
+    """--keep reads a header back into the tables the writer takes"""
+    sets = {0: {10: 8, 14: 9, 22: 17}, 1: {12: 9}}
+    tables = {0: {18: 17}, 1: {10: 10, 20: 17}}
+    p = tmp_path / "t.h"
+    p.write_text(tune_msm.header_text(sets, tables, "test gpu"))
+    assert tune_msm.committed_tables(str(p)) == (sets, tables)
