@@ -459,6 +459,7 @@ int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnes
     while ((int)ctx->lanes.size() < lanes) {
       std::unique_ptr<Ctx> lane(new Ctx());
       ctx_init(*lane, ctx->c.device);
+      lane->shared_gpu = true;
       ctx->lanes.push_back(std::move(lane));
     }
     // largest domains first (longest-processing-time order) so the tail is made of small proofs

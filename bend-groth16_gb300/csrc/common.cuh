@@ -138,6 +138,9 @@ struct NttTables {
 struct Ctx {
   int device = 0;
   int sm_count = 0;
+  // a lane of bg_prove_batch or of the server: other lanes' proofs share the GPU, so a proof
+  // keeps the throughput-oriented schedule even when it is small
+  bool shared_gpu = false;
   cudaStream_t stream = nullptr;          // main stream: every public call is ordered on it
   cudaStream_t side[kStreams] = {};       // concurrent MSMs inside a proof
   cudaStream_t copy = nullptr;            // uploads that overlap a proof (one-shot keys)

@@ -480,10 +480,11 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   // A small proof's accumulations together fill less than one wave of the GPU (short slices:
   // about entries / 8 threads each), so queueing them on one stream would leave it mostly
   // idle: each MSM then runs its whole chain -- accumulation, heavy pass, reduction -- on its
-  // own stream, and the five overlap.
+  // own stream, and the five overlap.  Not in a batch or server lane, where other proofs
+  // fill the GPU and the one-stream schedule's lighter reductions give more proofs per second.
   size_t acc_threads = 0;
   for (int j = 0; j < 5; j++) acc_threads += so[j]->max_entries / 8 + 1;
-  const bool overlap = acc_threads <= (size_t)ctx.sm_count * 4 * 128;
+  const bool overlap = !ctx.shared_gpu && acc_threads <= (size_t)ctx.sm_count * 4 * 128;
   for (int j = 0; j < 5; j++) {
     const Job& jb = jobs[j];
     cudaStream_t red = ctx.side[1 + j];

@@ -48,6 +48,7 @@ class Server {
     for (int i = 0; i < lanes; i++) {
       std::unique_ptr<Ctx> c(new Ctx());
       ctx_init(*c, device);
+      c->shared_gpu = lanes > 1;
       lanes_.push_back(std::move(c));
       reserved_.push_back(0);
       busy_.push_back(false);
