@@ -37,7 +37,7 @@ EXPORTS = (
     "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch", "bg_prove_footprint",
     "bg_server_create", "bg_server_submit", "bg_server_wait", "bg_server_reserved_bytes", "bg_server_destroy",
     "bg_ctx_timeline", "bg_msm_table_window_bits", "bg_ctx_transfer_bytes", "bg_verify", "bg_pairing",
-    "bg_msm_window_override",
+    "bg_msm_window_override", "bg_msm_proof_window_bits",
 )
 
 
@@ -110,6 +110,7 @@ def lib():
         "bg_synth_square_chain": (i32, [vp, u32, u64, ctypes.c_char_p]),
         "bg_msm_window_bits": (i32, [sz, i32]),
         "bg_msm_table_window_bits": (i32, [sz, i32]),
+        "bg_msm_proof_window_bits": (i32, [sz, i32]),
         "bg_msm_window_override": (i32, [vp, i32, i32, i32]),
         "bg_ctx_profile": (i32, [vp, i32]),
         "bg_ctx_timeline": (i32, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),

@@ -288,6 +288,7 @@ void bg_host_free(void* p) {
 
 int bg_msm_window_bits(size_t n, int curve) { return msm_pick_c(n, curve == BG_CURVE_G2); }
 int bg_msm_table_window_bits(size_t n, int curve) { return msm_pick_c_table(n, curve == BG_CURVE_G2); }
+int bg_msm_proof_window_bits(size_t n, int curve) { return msm_pick_c_proof(n, curve == BG_CURVE_G2); }
 
 int bg_msm_window_override(bg_ctx* ctx, int layout, int curve, int c) {
   if (!ctx || (layout != 0 && layout != 1) || (curve != BG_CURVE_G1 && curve != BG_CURVE_G2) ||

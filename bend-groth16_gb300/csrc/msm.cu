@@ -683,6 +683,11 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   msm_accumulate<F>(ctx, st, tag, d_points, so, plan, st_reduce, table);
 }
 
+int msm_pick_c_proof(size_t n, bool g2) {
+  if (const int t = tuned(kTuneProofSets, n, g2)) return t;
+  return msm_pick_c(n, g2);
+}
+
 int msm_pick_c_table(size_t n, bool g2) {
   // one shared bucket set: wider windows (fewer additions) at the price of 2^(c-1) buckets
   if (const int t = tuned(kTuneTables, n, g2)) return t;

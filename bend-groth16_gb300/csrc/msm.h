@@ -49,6 +49,8 @@ struct MsmSort {
 // window width for n points (the committed table of msm_tune.h, else a size rule)
 int msm_pick_c(size_t n, bool g2 = false);
 int msm_pick_c_table(size_t n, bool g2 = false);
+// window width of a bucket-set-per-window MSM inside a proof (one-shot proofs)
+int msm_pick_c_proof(size_t n, bool g2 = false);
 void msm_init_kernels();
 // allocate t.d (cudaMalloc) and fill it from n packed affine points on `st`; c = 0 picks the
 // window width from n

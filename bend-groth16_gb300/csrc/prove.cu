@@ -12,6 +12,7 @@
 // The QAP runs concurrently with the first accumulations.  The host finishes every MSM (window
 // Horner) as soon as its stream drains and assembles A, B and most of C (r delta, s delta,
 // s A + r B1, ...) while msm_h is still running, so only msm_h's finish is left at the end.
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <memory>
@@ -465,7 +466,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   std::vector<std::pair<SortKey, MsmSort>> sorts;
   sorts.reserve(5);
   auto sort_for = [&](const Job& jb, cudaStream_t s) -> const MsmSort& {
-    const int c_sets = ctx.c_override[0][jb.g2 ? 1 : 0] ? ctx.c_override[0][jb.g2 ? 1 : 0] : msm_pick_c(jb.n, jb.g2);
+    const int c_sets = ctx.c_override[0][jb.g2 ? 1 : 0] ? ctx.c_override[0][jb.g2 ? 1 : 0] : msm_pick_c_proof(jb.n, jb.g2);
     const SortKey k{jb.sc, jb.n, jb.tab ? jb.tab->c : c_sets, jb.tab != nullptr};
     for (auto& e : sorts)
       if (e.first.sc == k.sc && e.first.n == k.n && e.first.c == k.c && e.first.shared == k.shared) return e.second;
@@ -574,9 +575,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
 // ---------------------------------------------------------------- scratch footprint
 // Device bytes one proof's workspace needs (the buffers msm_launch, qap_h_run and
 // prove_resident request), used for admission control; a 10% margin covers rounding.
-static size_t msm_footprint(size_t n, bool g2) {
-  if (n == 0) return 0;
-  const int c = msm_pick_c(n, g2);
+static size_t msm_footprint_c(size_t n, bool g2, int c) {
   const size_t W = 254 / c + 1, nb = size_t(1) << (c - 1), nkeys = W * nb;
   const size_t PW = g2 ? 64 : 32;
   const size_t entries = n * W;
@@ -589,6 +588,10 @@ static size_t msm_footprint(size_t n, bool g2) {
   const size_t words = 3 * (nkeys + 1) + entries + nkeys * PW + 2 * threads * PW + threads / 8 + 2 +
                        W * J * 2 * PW + 2 * ((nkeys + 1) / 2048 + 1);
   return words * 4;
+}
+static size_t msm_footprint(size_t n, bool g2) {
+  if (n == 0) return 0;
+  return std::max(msm_footprint_c(n, g2, msm_pick_c(n, g2)), msm_footprint_c(n, g2, msm_pick_c_proof(n, g2)));
 }
 
 size_t prove_footprint(const Header& h) {

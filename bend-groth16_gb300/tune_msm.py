@@ -9,7 +9,10 @@ Two layouts are tuned, as the library uses them:
   * window tables of resident keys (one shared bucket set): whole SquareChain(2^K) proofs
     against a key uploaded with the table width of one curve forced to c in [rule - 1, rule + 1],
     widened the same way (every G1 query of that proof has floor(log2 n) = K, and so does the
-    G2 one), G1 first, then G2 with G1 at its best.
+    G2 one), G1 first, then G2 with G1 at its best;
+  * one bucket set per window inside a proof: whole one-shot SquareChain(2^K) proofs
+    (bg_prove_host) with one curve's width forced to c in [current - 2, current + 2], widened
+    the same way.
 Timings are medians of wall-clock calls of the synchronous API (device work included).  Sizes
 the run skips keep 0 in the table (the library's size rule applies there).
 """
@@ -119,21 +122,56 @@ def tune_tables(ctx, ks, data_root, reps, log):
 
 
 def committed_tables(path):
-    """the kTuneSets / kTuneTables rows of an existing header, as {curve: {log2 n: c}} (nonzero only)"""
+    """the kTuneSets / kTuneTables / kTuneProofSets rows of an existing header, as
+    {curve: {log2 n: c}} (nonzero only)"""
     import re
     rows = re.findall(r"\{([0-9, ]+)\}", open(path).read())
     out = []
-    for r in rows[:4]:
+    for r in rows[:6]:
         vals = [int(x) for x in r.split(",")]
         out.append({MIN_LOG2 + i: v for i, v in enumerate(vals) if v})
-    return {0: out[0], 1: out[1]}, {0: out[2], 1: out[3]}
+    while len(out) < 6:
+        out.append({})
+    return {0: out[0], 1: out[1]}, {0: out[2], 1: out[3]}, {0: out[4], 1: out[5]}
 
 
-def header_text(sets, tables, gpu):
+def tune_proof_sets(ctx, ks, data_root, reps, log):
+    """layout 2: whole one-shot proofs (every file uploaded, one bucket set per window) with one
+    curve's width forced; every G1 MSM of a SquareChain(2^K) proof has floor(log2 n) = K, and so
+    does the G2 one"""
+    best = {0: {}, 1: {}}
+    for k in ks:
+        path = os.path.join(data_root, "sq%d" % k)
+        if not os.path.exists(os.path.join(path, "vk.bin")):
+            ctx.synth_square_chain(k, 4242 + k, path)
+        files = bendg.HostFiles(path, pinned=True)
+        forced = {0: 0, 1: 0}
+        for curve in (bendg.CURVE_G1, bendg.CURVE_G2):
+            rule = bendg.lib().bg_msm_proof_window_bits(1 << k, curve)
+
+            def measure(c):
+                for cv in (0, 1):
+                    ctx.window_override(0, cv, forced[cv] if cv != curve else c)
+                return median_ms(lambda: ctx.prove_host(files), reps)
+            times = search(measure, rule - 2, rule + 2, 3, 20)
+            c_best = min(times, key=times.get)
+            forced[curve] = c_best
+            best[curve][k] = c_best
+            log("proof %s K=%d: %s -> c=%d" % ("g1" if curve == 0 else "g2", k,
+                                              " ".join("%d:%.3f" % kv for kv in sorted(times.items())), c_best))
+        for cv in (0, 1):
+            ctx.window_override(0, cv, 0)
+    return best
+
+
+def header_text(sets, tables, gpu, proof_sets=None):
+    proof_sets = proof_sets or {0: {}, 1: {}}
+
     def row(d):
         return "{" + ", ".join(str(d.get(lg, 0)) for lg in range(MIN_LOG2, MAX_LOG2 + 1)) + "}"
     return """// Window widths of the MSM per (log2 n, curve), measured on %s by bend-groth16_gb300/tune_msm.py
-// and committed; 0 = not measured, the size rule of msm_pick_c / msm_pick_c_table applies.
+// and committed; 0 = not measured, the size rule of msm_pick_c / msm_pick_c_table applies
+// (msm_pick_c_proof: the bucket-set-per-window entry).
 // Rows: [0] G1, [1] G2; columns: floor(log2 n) = kTuneMinLog2 .. kTuneMaxLog2.
 #pragma once
 
@@ -141,7 +179,7 @@ namespace bg {
 
 constexpr int kTuneMinLog2 = %d;
 constexpr int kTuneMaxLog2 = %d;
-// one bucket set per window (standalone MSMs, one-shot proofs)
+// one bucket set per window (standalone MSMs)
 constexpr signed char kTuneSets[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
     %s,
     %s};
@@ -149,9 +187,15 @@ constexpr signed char kTuneSets[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
 constexpr signed char kTuneTables[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
     %s,
     %s};
+// one bucket set per window inside a proof (one-shot proofs): the MSMs share the GPU with
+// each other's reductions and the QAP, which moves the best width from the standalone one
+constexpr signed char kTuneProofSets[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
+    %s,
+    %s};
 
 }  // namespace bg
-""" % (gpu, MIN_LOG2, MAX_LOG2, row(sets[0]), row(sets[1]), row(tables[0]), row(tables[1]))
+""" % (gpu, MIN_LOG2, MAX_LOG2, row(sets[0]), row(sets[1]), row(tables[0]), row(tables[1]),
+       row(proof_sets[0]), row(proof_sets[1]))
 
 
 def main():
@@ -161,6 +205,8 @@ def main():
     ap.add_argument("--data-root", default="/tmp/bg_tune")
     ap.add_argument("--max-sets-log2", type=int, default=22)
     ap.add_argument("--table-ks", default="10,12,14,16,18,20")
+    ap.add_argument("--proof-ks", default="10,12,14,16,18,20",
+                    help="K of the one-shot SquareChain(2^K) proofs that tune the in-proof widths")
     ap.add_argument("--keep", default=None,
                     help="an existing msm_tune.h whose entries are kept where this run measures nothing")
     args = ap.parse_args()
@@ -197,15 +243,17 @@ def main():
         sets = tune_sets(ctx, torch, pts_g1, pts_g2, range(MIN_LOG2, args.max_sets_log2 + 1),
                          range(MIN_LOG2, min(args.max_sets_log2, 20) + 1), args.reps, log)
     tables = tune_tables(ctx, [int(k) for k in args.table_ks.split(",") if k], args.data_root, args.reps, log)
+    proof_sets = tune_proof_sets(ctx, [int(k) for k in args.proof_ks.split(",") if k], args.data_root, args.reps,
+                                 log)
     if args.keep:
-        old_sets, old_tables = committed_tables(args.keep)
-        for new, old in ((sets, old_sets), (tables, old_tables)):
+        old_sets, old_tables, old_proof = committed_tables(args.keep)
+        for new, old in ((sets, old_sets), (tables, old_tables), (proof_sets, old_proof)):
             for curve in (0, 1):
                 for lg, c in old[curve].items():
                     new[curve].setdefault(lg, c)
     gpu = torch.cuda.get_device_name(0)
     with open(args.out, "w") as f:
-        f.write(header_text(sets, tables, gpu))
+        f.write(header_text(sets, tables, gpu, proof_sets))
     with open(os.path.splitext(args.out)[0] + ".log", "w") as f:
         f.write("\n".join(log_lines) + "\n")
     ctx.close()

@@ -221,9 +221,13 @@ int bg_msm_window_bits(size_t n, int curve);
 /* Window width c of the window tables a resident key (bg_pk_upload) builds for a query set of
  * n points: one shared bucket set of 2^(c-1) buckets, floor(254 / c) + 1 table rows. */
 int bg_msm_table_window_bits(size_t n, int curve);
+/* Window width c of a bucket-set-per-window MSM of n points inside a proof whose key has no
+ * window tables (bg_prove_dir, bg_prove_host): tuned on whole proofs, where the MSMs share the
+ * GPU with each other's reductions and the QAP; else bg_msm_window_bits. */
+int bg_msm_proof_window_bits(size_t n, int curve);
 /* Tuning hook: force the window width of later MSMs of this context, layout 0 = one bucket set
- * per window (bg_msm_*, one-shot proofs), 1 = window tables of keys uploaded afterwards;
- * c = 0 restores the library's choice, else 2..22. */
+ * per window (bg_msm_* and the MSMs of proofs without window tables), 1 = window tables of keys
+ * uploaded afterwards; c = 0 restores the library's choice, else 2..22. */
 int bg_msm_window_override(bg_ctx* ctx, int layout, int curve, int c);
 
 /* ---- measurement (no counterpart in the reference, which prints only T lines) ------- */

@@ -30,3 +30,4 @@ def test_status_strings(built_lib):
         assert L.bg_strerror(st)
     assert L.bg_msm_window_bits(1 << 20, 0) >= L.bg_msm_window_bits(1 << 10, 0)
     assert L.bg_msm_table_window_bits(1 << 18, 1) >= L.bg_msm_table_window_bits(1 << 10, 1)
+    assert 3 <= L.bg_msm_proof_window_bits(1 << 18, 1) <= 20

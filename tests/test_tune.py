@@ -35,7 +35,7 @@ def test_header_text_rows():
     tables = {0: {18: 17}, 1: {}}
     h = tune_msm.header_text(sets, tables, "test gpu")
     rows = re.findall(r"\{([0-9, ]+)\}", h)
-    assert len(rows) == 4
+    assert len(rows) == 6
     vals = [[int(x) for x in r.split(",")] for r in rows]
     assert all(len(v) == tune_msm.MAX_LOG2 - tune_msm.MIN_LOG2 + 1 for v in vals)
     assert vals[0][0] == 8 and vals[0][1] == 9 and vals[0][-1] == 17 and vals[0][5] == 0
@@ -49,7 +49,7 @@ def test_committed_header_is_in_range():
     import os
     src = open(os.path.join(os.path.dirname(tune_msm.__file__), "csrc", "msm_tune.h")).read()
     rows = re.findall(r"\{([0-9, ]+)\}", src)
-    assert len(rows) == 4
+    assert len(rows) == 6
     for r in rows:
         v = [int(x) for x in r.split(",")]
         assert len(v) == tune_msm.MAX_LOG2 - tune_msm.MIN_LOG2 + 1
@@ -60,6 +60,7 @@ def test_committed_tables_round_trip(tmp_path):
     """--keep reads a header back into the tables the writer takes"""
     sets = {0: {10: 8, 14: 9, 22: 17}, 1: {12: 9}}
     tables = {0: {18: 17}, 1: {10: 10, 20: 17}}
+    proof = {0: {}, 1: {18: 13}}
     p = tmp_path / "t.h"
-    p.write_text(tune_msm.header_text(sets, tables, "test gpu"))
-    assert tune_msm.committed_tables(str(p)) == (sets, tables)
+    p.write_text(tune_msm.header_text(sets, tables, "test gpu", proof))
+    assert tune_msm.committed_tables(str(p)) == (sets, tables, proof)
