@@ -492,6 +492,136 @@ __global__ void k_window_reduce(const uint32_t* __restrict__ offsets, const uint
   if (t == 0) store_xyzz(out + (size_t)blockIdx.x * 2 * PW, acc);
 }
 
+// The same reduction with the points a thread owns in shared memory (word i of thread t's
+// point at base[i * RT + t]): R, T and a staging column for the scan.  One out-of-line body
+// adds a point into another (and one doubles in place), so no point is live in registers
+// across a call.  The register-resident form above spills in G2 (R, T and the addend are
+// 3 x 64 words across inlined Fq2 additions: 2.4 KB of spill stores per thread); this one
+// leaves 0.4 KB, and an addition's latency falls with it (G2 MSM 2^18 5.59 -> 5.33 ms,
+// SquareChain(2^10) proof 1.24 -> 1.11 ms, 2^12 1.66 -> 1.46 ms, 2^18 10.74 -> 10.62 ms).  For
+// G1 (no spills either way) it was measured level, so G1 keeps the register form.
+BG_DEV void elem_load(Fq& e, const uint32_t* src, uint32_t stride) {
+#pragma unroll
+  for (int l = 0; l < 8; l++) e.v[l] = src[l * stride];
+}
+BG_DEV void elem_load(Fq2& e, const uint32_t* src, uint32_t stride) {
+  elem_load(e.c0, src, stride);
+  elem_load(e.c1, src + 8 * stride, stride);
+}
+BG_DEV void elem_store(uint32_t* dst, uint32_t stride, const Fq& e) {
+#pragma unroll
+  for (int l = 0; l < 8; l++) dst[l * stride] = e.v[l];
+}
+BG_DEV void elem_store(uint32_t* dst, uint32_t stride, const Fq2& e) {
+  elem_store(dst, stride, e.c0);
+  elem_store(dst + 8 * stride, stride, e.c1);
+}
+template <class F>
+BG_DEV void pt_load(XYZZ<F>& p, const uint32_t* src, uint32_t stride) {
+  constexpr int FW = FieldWords<F>::value;
+  elem_load(p.x, src, stride);
+  elem_load(p.y, src + FW * stride, stride);
+  elem_load(p.zz, src + 2 * FW * stride, stride);
+  elem_load(p.zzz, src + 3 * FW * stride, stride);
+}
+template <class F>
+BG_DEV void pt_store(uint32_t* dst, uint32_t stride, const XYZZ<F>& p) {
+  constexpr int FW = FieldWords<F>::value;
+  elem_store(dst, stride, p.x);
+  elem_store(dst + FW * stride, stride, p.y);
+  elem_store(dst + 2 * FW * stride, stride, p.zz);
+  elem_store(dst + 3 * FW * stride, stride, p.zzz);
+}
+// dst (stride) += src: shared memory with stride sstride, or a contiguous point in global
+// memory (sstride 1)
+template <class F>
+static __device__ __noinline__ void pt_add_into(uint32_t* dst, uint32_t stride, const uint32_t* src,
+                                                uint32_t sstride) {
+  XYZZ<F> p, q;
+  pt_load(p, dst, stride);
+  if (sstride == 1) q = load_xyzz<F>(src);
+  else pt_load(q, src, sstride);
+  pt_store(dst, stride, xyzz_add(p, q));
+}
+template <class F>
+static __device__ __noinline__ void pt_dbl_in(uint32_t* dst, uint32_t stride) {
+  XYZZ<F> p;
+  pt_load(p, dst, stride);
+  pt_store(dst, stride, xyzz_dbl(p));
+}
+// shared memory of k_window_reduce_sm: R, T and the scan's staging column
+template <class F>
+constexpr size_t reduce_sm_bytes(uint32_t RT) {
+  return 3 * (size_t)RT * 4 * FieldWords<F>::value * sizeof(uint32_t);
+}
+
+template <class F>
+__global__ void k_window_reduce_sm(const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ buckets,
+                                   const uint32_t* __restrict__ pieces, uint32_t K, uint32_t nb, uint32_t M,
+                                   uint32_t J, uint32_t* __restrict__ out) {
+  constexpr int PW = 4 * FieldWords<F>::value;
+  extern __shared__ uint32_t sm[];
+  const uint32_t RT = blockDim.x;
+  const uint32_t w = blockIdx.x / J, j = blockIdx.x % J, t = threadIdx.x;
+  const size_t key0 = (size_t)w * nb + ((size_t)j * RT + t) * M;
+  uint32_t* R = sm + t;                        // running sum R_t
+  uint32_t* T = sm + (size_t)PW * RT + t;      // weighted sum T_t
+  uint32_t* S = sm + (size_t)2 * PW * RT + t;  // staging for the scan
+  pt_store(R, RT, xyzz_inf<F>());
+  pt_store(T, RT, xyzz_inf<F>());
+  for (int k = (int)M - 1; k >= 0; k--) {
+    const size_t key = key0 + k;
+    const uint32_t o0 = offsets[key], o1 = offsets[key + 1];
+    if (o1 != o0) {
+      const uint32_t t0 = o0 / K, t1 = (o1 - 1) / K;
+      if (t0 == t1 || t1 - t0 > kPieceLimit) {
+        pt_add_into<F>(R, RT, buckets + key * PW, 1);
+      } else {
+        pt_add_into<F>(R, RT, pieces + (2 * (size_t)t0 + 1) * PW, 1);
+        for (uint32_t u = t0 + 1; u <= t1; u++) pt_add_into<F>(R, RT, pieces + 2 * (size_t)u * PW, 1);
+      }
+    }
+    pt_add_into<F>(T, RT, R, RT);
+  }
+  __syncthreads();
+  // inclusive suffix scan of R over the CTA (Hillis-Steele), through the staging column
+  for (uint32_t d = 1; d < RT; d <<= 1) {
+    if (t + d < RT) {
+#pragma unroll 8
+      for (int i = 0; i < PW; i++) S[i * RT] = R[i * RT + d];
+    } else {
+      pt_store(S, RT, xyzz_inf<F>());
+    }
+    __syncthreads();
+    pt_add_into<F>(R, RT, S, RT);
+    __syncthreads();
+  }
+  // R_j = Suf_0
+  if (t == 0) {
+#pragma unroll 8
+    for (int i = 0; i < PW; i++) out[((size_t)blockIdx.x * 2 + 1) * PW + i] = R[i * RT];
+  }
+  // Y_t = T_t + M Suf_t (t >= 1), Y_0 = T_0
+  if (t >= 1) {
+    for (uint32_t m = M; m > 1; m >>= 1) pt_dbl_in<F>(R, RT);
+    pt_add_into<F>(T, RT, R, RT);
+  }
+  __syncthreads();
+  for (uint32_t d = RT >> 1; d >= 1; d >>= 1) {
+    if (t < d) pt_add_into<F>(T, RT, T + d, RT);
+    __syncthreads();
+  }
+  if (t == 0) {
+#pragma unroll 8
+    for (int i = 0; i < PW; i++) out[(size_t)blockIdx.x * 2 * PW + i] = T[i * RT];
+  }
+}
+
+// which form reduces a field's windows (G1's register-resident form does not spill: 200
+// registers)
+template <class F>
+constexpr bool kReduceInSmem = FieldWords<F>::value == 16;
+
 // Shape of the window reduction: RT threads x M buckets per thread x J parts per window, picked
 // by a latency model.  A thread's dependent chain is M (2 + e / K) additions (each bucket
 // costs its pieces, about 1 + e / K for e entries per bucket, plus the running-sum addition),
@@ -509,8 +639,12 @@ int reduce_blocks_per_sm(uint32_t RT) {
   while ((1u << lrt) < RT) lrt++;
   if (!cache[lrt]) {
     int n = 0;
-    BG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_window_reduce<F>, (int)RT,
-                                                          RT * 4 * FieldWords<F>::value * sizeof(uint32_t)));
+    if constexpr (kReduceInSmem<F>)
+      BG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_window_reduce_sm<F>, (int)RT,
+                                                            reduce_sm_bytes<F>(RT)));
+    else
+      BG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_window_reduce<F>, (int)RT,
+                                                            RT * 4 * FieldWords<F>::value * sizeof(uint32_t)));
     cache[lrt] = n > 0 ? n : 1;
   }
   return cache[lrt];
@@ -661,8 +795,12 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)so.sets * J * 2 * PW);
   {
     KernelTimer kt(ctx, FW == 8 ? "msm_reduce_g1" : "msm_reduce_g2", rs);
-    k_window_reduce<F><<<so.sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(so.offsets, buckets, bs.parts, bs.K,
+    if constexpr (kReduceInSmem<F>)
+      k_window_reduce_sm<F><<<so.sets * J, RT, reduce_sm_bytes<F>(RT), rs>>>(so.offsets, buckets, bs.parts, bs.K,
                                                                              so.nb, M, J, parts);
+    else
+      k_window_reduce<F><<<so.sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(so.offsets, buckets, bs.parts, bs.K,
+                                                                               so.nb, M, J, parts);
     BG_CHECK_LAUNCH();
   }
   plan.fetch_stream = rs;
@@ -769,8 +907,10 @@ void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32) {
 void msm_init_kernels() {
   static bool done = false;
   if (done) return;
+  static_assert(!kReduceInSmem<Fq> && kReduceInSmem<Fq2>, "reduction forms: G1 in registers, G2 in shared memory");
   BG_CUDA(cudaFuncSetAttribute(k_window_reduce<Fq>, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 32 * 4));
-  BG_CUDA(cudaFuncSetAttribute(k_window_reduce<Fq2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 64 * 4));
+  BG_CUDA(cudaFuncSetAttribute(k_window_reduce_sm<Fq2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)reduce_sm_bytes<Fq2>(256)));
   done = true;
 }
 
