@@ -625,7 +625,33 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
     x = scalars(n1)
     res["ntt_2^20_forward_ms"] = timeit(lambda: ctx.ntt_dev(x.data_ptr(), 20, 0) or torch.cuda.synchronize())
     res["coset_ntt_2^20_ms"] = timeit(lambda: ctx.ntt_dev(x.data_ptr(), 20, 2) or torch.cuda.synchronize())
+    res["ntt_roofline"] = ntt_roofline(20, res["ntt_2^20_forward_ms"], imad_peak)
     return res
+
+
+def ntt_roofline(lg, ms, imad_peak):
+    """both bounds of a forward NTT of 2^lg Fr elements: HBM (each element read and written
+    once, 2 x 32 B) against the measured copy bandwidth, and the multiply-adds of its
+    butterflies ((n/2) log2 n Fr products of 232: a 512-bit Karatsuba product and one
+    Montgomery reduction) against the probed IMAD rate; the larger time is the binding bound"""
+    n = 1 << lg
+    hbm_gbs = None
+    pf = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pf):
+        hbm_gbs = json.load(open(pf)).get("hbm_gbs")
+    min_bytes = 2 * 32 * n
+    work = (n // 2) * lg * 232
+    t_imad = work / imad_peak * 1e3
+    t_hbm = min_bytes / (hbm_gbs * 1e9) * 1e3 if hbm_gbs else None
+    bound = "imad" if t_hbm is None or t_imad >= t_hbm else "hbm"
+    return {"n": n, "ms": ms, "bound": bound,
+            "imad": {"work": work, "bound_ms": round(t_imad, 4), "achieved_gimad_s": round(work / (ms * 1e-3) / 1e9, 1),
+                     "frac": round(t_imad / ms, 4), "peak_source": "bg_probe_imad"},
+            "hbm": {"min_bytes": min_bytes, "bound_ms": round(t_hbm, 4) if t_hbm else None,
+                    "moved_bytes_2_pass_plan": 2 * min_bytes,
+                    "achieved_gbs": round(2 * min_bytes / (ms * 1e-3) / 1e9, 1),
+                    "frac": round(t_hbm / ms, 4) if t_hbm else None,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}}
 
 
 # ---------------------------------------------------------------- CPU restatement

@@ -30,3 +30,15 @@ def test_shifted_witness_satisfies_square_chain(tmp_path):
 
 def test_batch_weights():
     assert abs(sum(bench.BATCH_WEIGHTS) - 1.0) < 1e-12 and len(bench.BATCH_KS) == 5
+
+
+def test_ntt_roofline_bounds():
+    """the NTT roofline reports both bounds; the multiply-add bound binds for a 2^20 transform"""
+    r = bench.ntt_roofline(20, 0.36, 13.1e12)
+    n = 1 << 20
+    assert r["imad"]["work"] == (n // 2) * 20 * 232
+    assert r["hbm"]["min_bytes"] == 64 * n
+    assert r["bound"] == "imad"
+    assert abs(r["imad"]["frac"] - r["imad"]["bound_ms"] / 0.36) < 1e-3
+    if r["hbm"]["bound_ms"] is not None:
+        assert r["hbm"]["bound_ms"] < r["imad"]["bound_ms"]
