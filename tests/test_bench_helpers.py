@@ -1,5 +1,6 @@
 """Host logic of bench.py (no GPU): the shifted SquareChain witnesses used for the 64-proof
-batch satisfy the circuit, and the instance generator's witness layout is what they assume."""
+batch satisfy the circuit, the instance generator's witness layout is what they assume, and the
+NTT roofline's two bounds."""
 import ctypes
 import os
 
