@@ -350,13 +350,13 @@ BG_DEV XYZZ<F> add_bucket(XYZZ<F> acc, const uint32_t* __restrict__ offsets, con
 // which half is hidden under other work, fitted to SquareChain(2^12..2^16) proofs).  Large MSMs
 // get 32-entry slices (throughput-bound, fewest pieces); small ones 8 (SquareChain(2^12) proof
 // 2.06 -> 1.69 ms, 2^14 2.44 -> 2.34 ms).
-inline uint32_t slice_entries(size_t max_entries, size_t nkeys) {
+inline uint32_t slice_entries(size_t max_entries, size_t nkeys, double piece_us = 4.5) {
   const double e = (double)max_entries / (double)(nkeys ? nkeys : 1);
   const double floor_us = (double)max_entries / 4580.0;
   uint32_t best = 32;
   double best_us = 1e300;
   for (uint32_t k = 4; k <= 32; k <<= 1) {
-    const double t = std::max(k * 6.6, floor_us) + (e / k + 2.0) * 4.5;
+    const double t = std::max(k * 6.6, floor_us) + (e / k + 2.0) * piece_us;
     if (t < best_us - 1e-9 || (t <= best_us + 1e-9 && k > best)) {
       best_us = t;
       best = k;
@@ -406,7 +406,10 @@ template <class F, class Get>
 BucketScratch bucket_scratch(size_t max_entries, size_t nkeys, Get get, uint32_t K = 0) {
   constexpr int PW = 4 * FieldWords<F>::value;
   BucketScratch b;
-  b.K = K ? K : whole_wave_slices<F>(max_entries, slice_entries(max_entries, nkeys));
+  // a G2 piece costs a G2 addition in the reduction: about twice a G1 one relative to the
+  // accumulation's mixed additions (SquareChain(2^12): G2 slices of 16 instead of 8)
+  const double piece_us = FieldWords<F>::value == 16 ? 9.0 : 4.5;
+  b.K = K ? K : whole_wave_slices<F>(max_entries, slice_entries(max_entries, nkeys, piece_us));
   const size_t s = bucket_slices(max_entries, b.K);
   b.parts = get("parts", 2 * s * PW);
   b.heavy = get("heavy", s / kPieceLimit + 2);
