@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the Poisson-arrival serving measurement")
     ap.add_argument("--msm-only", action="store_true",
                     help="time only the standalone G1 MSM 2^20 (a small, single-kernel-family profiling target)")
+    ap.add_argument("--ntt-only", action="store_true",
+                    help="time only the forward NTT of 2^20 Fr elements (a single-kernel profiling target)")
     ap.add_argument("--data-root", default=os.environ.get("BG_BENCH_DATA", "/tmp/bg_bench"))
     return ap.parse_args()
 
@@ -175,6 +177,26 @@ def run_ours(args, dist: Dist):
     torch.cuda.set_device(dist.local)
     ctx = bendg.Context(dist.local)
     L = bendg.lib()
+    if args.ntt_only:
+        # seeded Fr elements below 2^252 (< r), Montgomery form irrelevant to the transform's cost
+        g = torch.Generator(device="cpu").manual_seed(args.seed)
+        x = torch.randint(0, 1 << 30, ((1 << 20) * 8,), dtype=torch.int32, generator=g).cuda()
+        x.view(-1, 8)[:, 7] &= 0x0FFFFFFF
+        ext = torch.cuda.ExternalStream(ctx.stream)
+        out = []
+        for i in range(max(3, args.warmup) + args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            ctx.ntt_dev(x.data_ptr(), 20, 0)
+            e1.record(ext)
+            e1.synchronize()
+            if i >= max(3, args.warmup):
+                out.append(e0.elapsed_time(e1))
+        ms = statistics.median(out)
+        ops, pms = ctx.probe_imad(0, 4096)
+        ctx.close()
+        return {"metric": "NTT 2^20 forward ms", "value": round(ms, 4), "unit": "ms", "higher_is_better": False,
+                "roofline": ntt_roofline(20, round(ms, 4), ops / (pms * 1e-3))}
     path = ensure_instance(args, dist, lambda k, s, p: ctx.synth_square_chain(k, s, p))
     files = bendg.HostFiles(path, pinned=True)
     hdr = files.words("header")
