@@ -294,10 +294,6 @@ PkDev* pk_stage_oneshot(Ctx& ctx, const bg_inputs& in) {
   pk->h = h;
   pk->pooled = true;
   try {
-    cudaStream_t st = ctx.stream;
-    upload_csr(ctx, in.r1cs_a, h.nc, pk->ca, st, true, "ca");
-    upload_csr(ctx, in.r1cs_b, h.nc, pk->cb, st, true, "cb");
-    upload_csr(ctx, in.r1cs_c, h.nc, pk->cc, st, true, "cc");
     const uint32_t* g1 = words(in.pk_g1);
     const uint32_t* g2 = words(in.pk_g2);
     pk->alpha = host_affine_from_wire<FqOps>(g1);
@@ -305,11 +301,13 @@ PkDev* pk_stage_oneshot(Ctx& ctx, const bg_inputs& in) {
     pk->delta = host_affine_from_wire<FqOps>(g1 + 64);
     pk->beta2 = host_affine_from_wire<Fq2Ops>(g2);
     pk->delta2 = host_affine_from_wire<Fq2Ops>(g2 + 64);
-    // the query sets in the order the proof's accumulations use them (a, b1, b2, l, h), each
-    // with its own staging buffer so no transfer waits for an earlier repack
+    // Everything goes up on the copy stream, in the order the proof needs it: the query sets
+    // of the first two accumulations (a, b1), then the R1CS matrices (the evaluations and the
+    // QAP, which feed only msm_h, the last accumulation), then b2, l and h.  The witness
+    // travels on the main stream meanwhile, so the shared sort of a, b1 and b2 starts as
+    // soon as the canonical scalars exist.  Each set has its own staging buffer, so no
+    // transfer waits for an earlier repack.
     cudaStream_t cs = ctx.copy;
-    BG_CUDA(cudaEventRecord(ctx.event("oneshot.csr"), st));
-    BG_CUDA(cudaStreamWaitEvent(cs, ctx.event("oneshot.csr"), 0));
     struct Set {
       int idx;
       const void* src;
@@ -325,6 +323,13 @@ PkDev* pk_stage_oneshot(Ctx& ctx, const bg_inputs& in) {
       upload_points(ctx, q.src, q.n, q.words, *q.dst, cs, true, q.tag);
       pk->ready[q.idx] = ctx.event(std::string("oneshot.ready.") + q.tag);
       BG_CUDA(cudaEventRecord(pk->ready[q.idx], cs));
+      if (q.idx == 1) {
+        upload_csr(ctx, in.r1cs_a, h.nc, pk->ca, cs, true, "ca");
+        upload_csr(ctx, in.r1cs_b, h.nc, pk->cb, cs, true, "cb");
+        upload_csr(ctx, in.r1cs_c, h.nc, pk->cc, cs, true, "cc");
+        pk->csr_ready = ctx.event("oneshot.csr");
+        BG_CUDA(cudaEventRecord(pk->csr_ready, cs));
+      }
     }
   } catch (...) {
     pk_free(pk);
@@ -401,6 +406,10 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   h2d(ctx, 1, z_wire, witness16, nz * 64, st);
   wire_to_packed(st, z_wire, z, nz, ctx.d_status);
   t_load.stop(st);
+  // the MSM scalars (canonical z) first: the sorts need nothing else
+  fr_from_mont(st, z, zc, nz);
+  cudaEvent_t ev_scalars = ctx.event("prove.scalars");
+  BG_CUDA(cudaEventRecord(ev_scalars, st));
 
   // ---- evals + canonical scalars
   t_evals.start(st);
@@ -409,18 +418,17 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   uint32_t* ec = ws.get_t<uint32_t>("prove.ec", d * 8);
   const CsrDev* m[3] = {&pk.ca, &pk.cb, &pk.cc};
   uint32_t* ev[3] = {ea, eb, ec};
+  if (pk.csr_ready) BG_CUDA(cudaStreamWaitEvent(st, pk.csr_ready, 0));
   std::unique_ptr<KernelTimer> kt_evals(new KernelTimer(ctx, "evals", st));
   for (int k = 0; k < 3; k++) {
     k_evals<<<ceil_div(d, 128), 128, 0, st>>>(m[k]->offs, m[k]->cols, m[k]->coeffs, z, (uint32_t)nz, h.nc,
                                               k == 0 ? h.ni : 0, d, ev[k], ctx.d_status);
     BG_CHECK_LAUNCH();
   }
-  fr_from_mont(st, z, zc, nz);
   kt_evals.reset();
   t_evals.stop(st);
 
   // ---- QAP on the main stream; it needs only the evaluation vectors
-  BG_CUDA(cudaEventRecord(ctx.ev_fork, st));
   t_qap.start(st);
   uint32_t* hh = ws.get_t<uint32_t>("prove.h", d * 8);
   uint32_t* hc = ws.get_t<uint32_t>("prove.hc", d * 8);
@@ -456,7 +464,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   // runs the five accumulations back to back, each waiting only for its own sort.
   cudaStream_t acc_st = ctx.side[0];
   cudaStream_t sort_st = ctx.side[kSortStream];
-  BG_CUDA(cudaStreamWaitEvent(sort_st, ctx.ev_fork, 0));
+  BG_CUDA(cudaStreamWaitEvent(sort_st, ev_scalars, 0));
   struct SortKey {
     const uint32_t* sc;
     size_t n;
@@ -477,7 +485,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   const MsmSort* so[5];
   for (int j = 0; j < 4; j++) so[j] = &sort_for(jobs[j], sort_st);
   so[4] = &sort_for(jobs[4], st);  // st: after the QAP
-  BG_CUDA(cudaStreamWaitEvent(acc_st, ctx.ev_fork, 0));
+  BG_CUDA(cudaStreamWaitEvent(acc_st, ev_scalars, 0));
   // A small proof's accumulations together fill less than one wave of the GPU (short slices:
   // about entries / 8 threads each), so queueing them on one stream would leave it mostly
   // idle: each MSM then runs its whole chain -- accumulation, heavy pass, reduction -- on its
@@ -493,7 +501,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     MsmPlan& p = plan[jb.idx];
     // only msm_h's reduction is not hidden under a later accumulation; overlapped, none is
     p.latency_critical = overlap || j == 4;
-    if (overlap) BG_CUDA(cudaStreamWaitEvent(ast, ctx.ev_fork, 0));
+    if (overlap) BG_CUDA(cudaStreamWaitEvent(ast, ev_scalars, 0));
     if (pk.ready[jb.idx]) BG_CUDA(cudaStreamWaitEvent(ast, pk.ready[jb.idx], 0));
     t_msm[jb.idx].start(ast);
     if (jb.g2) {

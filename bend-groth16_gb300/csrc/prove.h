@@ -32,6 +32,8 @@ struct PkDev {
   // points of each query set (a, b1, b2, h, l) still arriving on the copy stream until ready[i]
   bool pooled = false;
   cudaEvent_t ready[5] = {};
+  // one-shot keys: the R1CS matrices arrive on the copy stream too, after the first query sets
+  cudaEvent_t csr_ready = nullptr;
 };
 
 Header parse_header(const bg_inputs& in);
