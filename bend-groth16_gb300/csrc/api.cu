@@ -165,9 +165,7 @@ void ctx_init(Ctx& c, int device) {
   BG_CUDA(cudaStreamCreateWithPriority(&c.copy, cudaStreamNonBlocking, least));
   for (int i = 0; i < kStreams; i++) {
     BG_CUDA(cudaStreamCreateWithPriority(&c.side[i], cudaStreamNonBlocking, i == 0 ? least : greatest));
-    BG_CUDA(cudaEventCreateWithFlags(&c.ev_join[i], cudaEventDisableTiming));
   }
-  BG_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
   c.d_status = c.ws.get_t<uint32_t>("status", 1);
   BG_CUDA(cudaMemsetAsync(c.d_status, 0, 4, c.stream));
   BG_CUDA(cudaStreamSynchronize(c.stream));
@@ -187,11 +185,7 @@ void ctx_release(Ctx& c) {
       cudaStreamDestroy(c.side[i]);
       c.side[i] = nullptr;
     }
-    if (c.ev_join[i]) cudaEventDestroy(c.ev_join[i]);
-    c.ev_join[i] = nullptr;
   }
-  if (c.ev_fork) cudaEventDestroy(c.ev_fork);
-  c.ev_fork = nullptr;
   for (auto& kv : c.events) cudaEventDestroy(kv.second);
   c.events.clear();
   for (const Ctx::Span& sp : c.spans) {

@@ -144,8 +144,6 @@ struct Ctx {
   cudaStream_t stream = nullptr;          // main stream: every public call is ordered on it
   cudaStream_t side[kStreams] = {};       // concurrent MSMs inside a proof
   cudaStream_t copy = nullptr;            // uploads that overlap a proof (one-shot keys)
-  cudaEvent_t ev_fork = nullptr;
-  cudaEvent_t ev_join[kStreams] = {};
   Workspace ws;
   PinnedBuf pinned[4];
   PinnedCache host_cache;

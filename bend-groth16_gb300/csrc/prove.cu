@@ -4,14 +4,18 @@
 // (Ev.matrix / matrix_a, groth16.bend:162-188, then Sc.canon, :214), qap (Pr.qap,
 // prove.bend:52-56), the five MSMs (prove.bend:64-117) and Groth.combine (groth16.bend:298-308).
 //
-// Device schedule (one context, the main stream + six side streams):
-//   main:   witness H2D + repack -> evals (3 CSR SpMV) -> z canonical -> qap_h -> h canonical
-//   side0:  MSM front ends and accumulations back to back (each fills the GPU):
-//           msm_a, msm_b1, msm_b2 (G2), msm_l (scalars z[ni..]), then msm_h once h is ready
-//   side1..5: each MSM's window reduction and result copy, overlapping the next accumulation
-// The QAP runs concurrently with the first accumulations.  The host finishes every MSM (window
-// Horner) as soon as its stream drains and assembles A, B and most of C (r delta, s delta,
-// s A + r B1, ...) while msm_h is still running, so only msm_h's finish is left at the end.
+// Device schedule (one context, the main stream + seven side streams + a copy stream):
+//   main:   witness H2D + repack -> z canonical -> evals (3 CSR SpMV) -> qap_h -> h canonical
+//           -> msm_h's sort
+//   side6:  the sorts of msm_a / msm_b1 / msm_b2 (shared) and msm_l, once z canonical exists
+//   side0:  accumulations back to back (each fills the GPU): msm_a, msm_b1, msm_b2 (G2),
+//           msm_l (scalars z[ni..]), then msm_h once h is sorted
+//   side1..5: each MSM's heavy-bucket pass, window reduction and result copy, overlapping the
+//           next accumulation (small proofs: each MSM's whole chain on its side stream)
+//   copy:   one-shot keys only: query sets and R1CS matrices in the order they are needed
+// The QAP runs concurrently with the first accumulations.  The host finishes every MSM as soon
+// as its stream drains and assembles A, B and most of C (r delta, s delta, s A + r B1, ...)
+// while msm_h is still running, so only msm_h's finish is left at the end.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
