@@ -415,7 +415,88 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   cudaEvent_t ev_scalars = ctx.event("prove.scalars");
   BG_CUDA(cudaEventRecord(ev_scalars, st));
 
-  // ---- evals + canonical scalars
+  // ---- the MSMs whose scalars are the assignment go first (host launch order matters for
+  // small proofs, whose kernels are shorter than the host's launches): msm_a, msm_b1, msm_b2,
+  // msm_l; msm_h follows the QAP
+  uint32_t* hh = ws.get_t<uint32_t>("prove.h", d * 8);
+  uint32_t* hc = ws.get_t<uint32_t>("prove.hc", d * 8);
+  MsmPlan plan[5];  // a, b1, b2, h, l
+  struct Job {
+    int idx;
+    const char* tag;
+    bool g2;
+    const uint32_t* pts;
+    const uint32_t* sc;
+    size_t n;
+    const MsmTable* tab;  // the query set's window table (resident keys), else null
+  };
+  auto tab = [&](int k) -> const MsmTable* { return pk.tables && pk.tab[k].d ? &pk.tab[k] : nullptr; };
+  const Job jobs[5] = {{0, "msm_a", false, pk.pa, zc, h.na, tab(0)},
+                       {1, "msm_b1", false, pk.pb1, zc, h.nb, tab(1)},
+                       {2, "msm_b2", true, pk.pb2, zc, h.nb, tab(2)},
+                       {4, "msm_l", false, pk.pl, zc + 8 * (size_t)h.ni, h.nl, tab(4)},
+                       {3, "msm_h", false, pk.ph, hc, h.nh, tab(3)}};
+  auto width = [&](const Job& jb) {
+    if (jb.tab) return jb.tab->c;
+    const int forced = ctx.c_override[0][jb.g2 ? 1 : 0];
+    return forced ? forced : msm_pick_c_proof(jb.n, jb.g2);
+  };
+  // Bucket orders on their own stream: a, b1 and b2 take the same scalars (the whole
+  // assignment) and, with equal lengths, the same window layout, so they share one sort; l's
+  // follows; h's is made on the main stream once the QAP is done.  The accumulation stream then
+  // runs the five accumulations back to back, each waiting only for its own sort.
+  cudaStream_t acc_st = ctx.side[0];
+  cudaStream_t sort_st = ctx.side[kSortStream];
+  BG_CUDA(cudaStreamWaitEvent(sort_st, ev_scalars, 0));
+  struct SortKey {
+    const uint32_t* sc;
+    size_t n;
+    int c;
+    bool shared;
+  };
+  std::vector<std::pair<SortKey, MsmSort>> sorts;
+  sorts.reserve(5);
+  auto sort_for = [&](const Job& jb, cudaStream_t s) -> const MsmSort& {
+    const SortKey k{jb.sc, jb.n, width(jb), jb.tab != nullptr};
+    for (auto& e : sorts)
+      if (e.first.sc == k.sc && e.first.n == k.n && e.first.c == k.c && e.first.shared == k.shared) return e.second;
+    sorts.emplace_back(k, MsmSort());
+    msm_sort(ctx, s, std::string(jb.tag) + ".sort", jb.sc, jb.n, k.c, k.shared, sorts.back().second);
+    return sorts.back().second;
+  };
+  BG_CUDA(cudaStreamWaitEvent(acc_st, ev_scalars, 0));
+  // A small proof's accumulations together fill less than one wave of the GPU (short slices:
+  // about entries / 8 threads each), so queueing them on one stream would leave it mostly
+  // idle: each MSM then runs its whole chain -- accumulation, heavy pass, reduction -- on its
+  // own stream, and the five overlap.  Not in a batch or server lane, where other proofs
+  // fill the GPU and the one-stream schedule's lighter reductions give more proofs per second.
+  size_t acc_threads = 0;
+  for (const Job& jb : jobs) acc_threads += jb.n * (size_t)(254 / width(jb) + 1) / 8 + 1;
+  const bool overlap = !ctx.shared_gpu && acc_threads <= (size_t)ctx.sm_count * 4 * 128;
+  auto launch = [&](int j, const MsmSort& so) {
+    const Job& jb = jobs[j];
+    cudaStream_t red = ctx.side[1 + j];
+    cudaStream_t ast = overlap ? red : acc_st;
+    MsmPlan& p = plan[jb.idx];
+    // only msm_h's reduction is not hidden under a later accumulation; overlapped, none is
+    p.latency_critical = overlap || j == 4;
+    if (overlap) BG_CUDA(cudaStreamWaitEvent(ast, ev_scalars, 0));
+    if (pk.ready[jb.idx]) BG_CUDA(cudaStreamWaitEvent(ast, pk.ready[jb.idx], 0));
+    t_msm[jb.idx].start(ast);
+    if (jb.g2) {
+      msm_accumulate<Fq2>(ctx, ast, jb.tag, jb.pts, so, p, red, jb.tab);
+      msm_fetch<Fq2>(ctx, ast, p);
+    } else {
+      msm_accumulate<Fq>(ctx, ast, jb.tag, jb.pts, so, p, red, jb.tab);
+      msm_fetch<Fq>(ctx, ast, p);
+    }
+    t_msm[jb.idx].stop(red);
+  };
+  const MsmSort* so[4];
+  for (int j = 0; j < 4; j++) so[j] = &sort_for(jobs[j], sort_st);
+  for (int j = 0; j < 4; j++) launch(j, *so[j]);
+
+  // ---- evals
   t_evals.start(st);
   uint32_t* ea = ws.get_t<uint32_t>("prove.ea", d * 8);
   uint32_t* eb = ws.get_t<uint32_t>("prove.eb", d * 8);
@@ -434,8 +515,6 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
 
   // ---- QAP on the main stream; it needs only the evaluation vectors
   t_qap.start(st);
-  uint32_t* hh = ws.get_t<uint32_t>("prove.h", d * 8);
-  uint32_t* hc = ws.get_t<uint32_t>("prove.hc", d * 8);
   {
     KernelTimer kt(ctx, "qap", st);
     qap_h_run(ctx, st, ea, eb, ec, hh, h.lg);
@@ -443,80 +522,8 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   }
   t_qap.stop(st);
 
-  // ---- MSM accumulations back to back on one stream (each one fills the GPU), every window
-  // reduction on a stream of its own so it overlaps the next accumulation; msm_h goes last
-  // because it waits for h
-  MsmPlan plan[5];  // a, b1, b2, h, l
-  struct Job {
-    int idx;
-    const char* tag;
-    bool g2;
-    const uint32_t* pts;
-    const uint32_t* sc;
-    size_t n;
-    const MsmTable* tab;  // the query set's window table (resident keys), else null
-  };
-  auto tab = [&](int k) -> const MsmTable* { return pk.tables && pk.tab[k].d ? &pk.tab[k] : nullptr; };
-  const Job jobs[5] = {{0, "msm_a", false, pk.pa, zc, h.na, tab(0)},
-                       {1, "msm_b1", false, pk.pb1, zc, h.nb, tab(1)},
-                       {2, "msm_b2", true, pk.pb2, zc, h.nb, tab(2)},
-                       {4, "msm_l", false, pk.pl, zc + 8 * (size_t)h.ni, h.nl, tab(4)},
-                       {3, "msm_h", false, pk.ph, hc, h.nh, tab(3)}};
-  // Bucket orders first, on their own stream: a, b1 and b2 take the same scalars (the whole
-  // assignment) and, with equal lengths, the same window layout, so they share one sort; l's
-  // follows; h's is made on the main stream once the QAP is done.  The accumulation stream then
-  // runs the five accumulations back to back, each waiting only for its own sort.
-  cudaStream_t acc_st = ctx.side[0];
-  cudaStream_t sort_st = ctx.side[kSortStream];
-  BG_CUDA(cudaStreamWaitEvent(sort_st, ev_scalars, 0));
-  struct SortKey {
-    const uint32_t* sc;
-    size_t n;
-    int c;
-    bool shared;
-  };
-  std::vector<std::pair<SortKey, MsmSort>> sorts;
-  sorts.reserve(5);
-  auto sort_for = [&](const Job& jb, cudaStream_t s) -> const MsmSort& {
-    const int c_sets = ctx.c_override[0][jb.g2 ? 1 : 0] ? ctx.c_override[0][jb.g2 ? 1 : 0] : msm_pick_c_proof(jb.n, jb.g2);
-    const SortKey k{jb.sc, jb.n, jb.tab ? jb.tab->c : c_sets, jb.tab != nullptr};
-    for (auto& e : sorts)
-      if (e.first.sc == k.sc && e.first.n == k.n && e.first.c == k.c && e.first.shared == k.shared) return e.second;
-    sorts.emplace_back(k, MsmSort());
-    msm_sort(ctx, s, std::string(jb.tag) + ".sort", jb.sc, jb.n, k.c, k.shared, sorts.back().second);
-    return sorts.back().second;
-  };
-  const MsmSort* so[5];
-  for (int j = 0; j < 4; j++) so[j] = &sort_for(jobs[j], sort_st);
-  so[4] = &sort_for(jobs[4], st);  // st: after the QAP
-  BG_CUDA(cudaStreamWaitEvent(acc_st, ev_scalars, 0));
-  // A small proof's accumulations together fill less than one wave of the GPU (short slices:
-  // about entries / 8 threads each), so queueing them on one stream would leave it mostly
-  // idle: each MSM then runs its whole chain -- accumulation, heavy pass, reduction -- on its
-  // own stream, and the five overlap.  Not in a batch or server lane, where other proofs
-  // fill the GPU and the one-stream schedule's lighter reductions give more proofs per second.
-  size_t acc_threads = 0;
-  for (int j = 0; j < 5; j++) acc_threads += so[j]->max_entries / 8 + 1;
-  const bool overlap = !ctx.shared_gpu && acc_threads <= (size_t)ctx.sm_count * 4 * 128;
-  for (int j = 0; j < 5; j++) {
-    const Job& jb = jobs[j];
-    cudaStream_t red = ctx.side[1 + j];
-    cudaStream_t ast = overlap ? red : acc_st;
-    MsmPlan& p = plan[jb.idx];
-    // only msm_h's reduction is not hidden under a later accumulation; overlapped, none is
-    p.latency_critical = overlap || j == 4;
-    if (overlap) BG_CUDA(cudaStreamWaitEvent(ast, ev_scalars, 0));
-    if (pk.ready[jb.idx]) BG_CUDA(cudaStreamWaitEvent(ast, pk.ready[jb.idx], 0));
-    t_msm[jb.idx].start(ast);
-    if (jb.g2) {
-      msm_accumulate<Fq2>(ctx, ast, jb.tag, jb.pts, *so[j], p, red, jb.tab);
-      msm_fetch<Fq2>(ctx, ast, p);
-    } else {
-      msm_accumulate<Fq>(ctx, ast, jb.tag, jb.pts, *so[j], p, red, jb.tab);
-      msm_fetch<Fq>(ctx, ast, p);
-    }
-    t_msm[jb.idx].stop(red);
-  }
+  // ---- msm_h: its sort on the main stream after the QAP, then its accumulation last
+  launch(4, sort_for(jobs[4], st));
 
   // ---- host work that needs no MSM result, overlapped with the device
   uint64_t r[4], s[4], rs[4];
