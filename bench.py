@@ -36,7 +36,8 @@ sys.path.insert(0, PKG)
 
 METRIC = "SquareChain 2^18 ms/proof"
 UNIT = "ms/proof"
-# BASELINE.md: the reference's own GPU path (Bend 2 CUDA, RTX 5090) at K=18, T total
+# the reference's own GPU path (Bend 2 CUDA, RTX 5090) at K=18, T total
+# (bend2/bench/prover_results.md:63, README.md:57)
 REF_GPU_K18_MS = 56083.0
 # 32-bit multiply-adds (mad.lo + mad.hi) the accumulation kernel executes per mixed addition
 # (madd-2008-s), from the products of fp_wide.cuh: a 512-bit Karatsuba product 3 x 32 = 96,
@@ -331,7 +332,7 @@ def run_ours(args, dist: Dist):
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(value * dist.world, 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": round(value / REF_GPU_K18_MS, 6),
-        "vs_baseline_ref": "Bend 2 CUDA path, RTX 5090, K=18 T total 56083 ms (BASELINE.md)",
+        "vs_baseline_ref": "Bend 2 CUDA path, RTX 5090, K=18 T total 56083 ms (bend2/bench/prover_results.md:63)",
         "dtype": "u32 (exact BN254 Fr/Fq Montgomery arithmetic)", "data": "synthetic (seeded SquareChain instance)",
         "config": {"workload": "SquareChain(2^%d) Groth16 proof: 4 G1 MSMs + 1 G2 MSM + 7 radix-2 NTTs of 2^%d"
                                % (args.log2n, lg),
