@@ -382,7 +382,7 @@ def shifted_witness(z_words, m: int):
 
 
 def batched(ctx, args, flush, ext):
-    """BASELINE configuration 3: 64 proofs of mixed K, one bg_prove_batch call versus the same
+    """The batch workload: 64 proofs of mixed K, one bg_prove_batch call versus the same
     proofs made one at a time (plain), both against resident keys; every batched proof must
     equal its plain twin bit for bit."""
     import random
@@ -463,7 +463,7 @@ def percentile(xs, q):
 
 
 def single_proofs(ctx, key, path, reps=5):
-    """BASELINE configuration 2 at its larger size: plain one-at-a-time proofs against a
+    """The single-proof workload at its larger size (2^20 constraints): plain one-at-a-time proofs against a
     resident key (wall time of the synchronous call, device work included), and the pairing
     check of the last one under the instance's vk.bin"""
     import numpy as np
@@ -490,7 +490,7 @@ def single_proofs(ctx, key, path, reps=5):
 
 
 def serving(ctx, args, lanes=8, seconds=1.5):
-    """BASELINE configuration 4: Poisson arrivals of prove requests with K drawn from
+    """The serving workload: Poisson arrivals of prove requests with K drawn from
     SERVE_KS, all five proving keys resident, continuous batching in the library's server;
     p50 / p99 latency (submit -> proof) and completed proofs/s per offered rate."""
     import random

@@ -1,4 +1,4 @@
-"""Batched proving (BASELINE configuration 3 shape: many proofs of uneven K in one call):
+"""Batched proving (the batch workload's shape: many proofs of uneven K in one call):
 every proof in the mix is bit-identical to the same proof made alone, and valid."""
 import os
 import random

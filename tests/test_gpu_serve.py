@@ -1,4 +1,4 @@
-"""The serving loop (BASELINE configuration 4 shape): requests of different K submitted while
+"""The serving loop (the serving workload's shape): requests of different K submitted while
 others are proving are admitted as lanes and memory free up; every result is the same proof
 made alone; a tight HBM budget serialises admission; an over-budget request is refused."""
 import random
