@@ -463,9 +463,9 @@ def percentile(xs, q):
 
 
 def single_proofs(ctx, key, path, reps=5):
-    """The single-proof workload at its larger size (2^20 constraints): plain one-at-a-time proofs against a
-    resident key (wall time of the synchronous call, device work included), and the pairing
-    check of the last one under the instance's vk.bin"""
+    """The single-proof workload at its larger size (2^20 constraints): plain one-at-a-time
+    proofs against a resident key (wall time of the synchronous call, device work included),
+    and the pairing check of the last one under the instance's vk.bin"""
     import numpy as np
 
     import bendg
