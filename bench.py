@@ -571,7 +571,7 @@ def serving(ctx, args, lanes=8, seconds=1.5):
 
 
 def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
-    """standalone primitives of the second benchmark configuration: G1 MSM 2^20, G2 MSM 2^18,
+    """the standalone primitives: G1 MSM 2^20, G2 MSM 2^18,
     NTT 2^20, all device-resident (points: the instance's h_query twice, as the reference's own
     MSM bench does for 2^20, bend2/bench/msm.bend:1-9; scalars uniform < r)"""
     import numpy as np
