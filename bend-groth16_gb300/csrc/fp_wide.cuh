@@ -11,7 +11,8 @@
 // before subtracting, which keeps them non-negative and below 4 p^2 < p R (4p < 2^256 for the
 // BN254 base field).
 //
-// The chains are written out limb by limb (generated): each asm block is one carry chain.
+// The chains are written out limb by limb: each asm block is one carry chain.  The host test
+// tests/device_emul.py executes these chains instruction by instruction on the CPU.
 #pragma once
 // included at the end of fp.cuh (needs Fp, Fq, Fq2 and reduce_once)
 
