@@ -4,7 +4,9 @@ CIOS product, squaring product, inverse and Montgomery -> canonical; the 512-bit
 squaring products over the whole 256-bit operand range; the Montgomery reduction over its whole
 input range [0, p R); the lazy-reduction forms a b - c d; Fq2 (bend2/src/fq2.bend:31-50); the
 XYZZ formulas of G1 and G2 with every special case (infinity on either side, P = Q, P = -Q).
-Every asm statement must also set the carry flag before reading it.  No GPU is involved."""
+The committed golden vectors (field ops, the 1000 Montgomery pairs, G1/G2 ops) go through the
+same emulated functions.  Every asm statement must also set the carry flag before reading it.
+No GPU is involved."""
 import random
 
 import pytest
@@ -247,3 +249,75 @@ def test_emulation_flags_an_unset_carry(tmp_path):
     assert d.fault() == 0
     d.call("fq_add", [d.words(1), d.words(2)], 8)
     assert d.fault() != 0
+
+
+def _records(name, cols):
+    import os
+    import struct
+
+    import numpy as np
+    from conftest import GOLDEN
+    buf = open(os.path.join(GOLDEN, *name), "rb").read()
+    (n,) = struct.unpack_from("<I", buf, 0)
+    return np.frombuffer(buf, dtype="<u4", offset=4).reshape(n, cols).astype(np.uint32)
+
+
+def _v16(words) -> int:
+    """a bend2/FORMAT.md field element (16 words of 16-bit limbs) as an integer"""
+    return o.from_words16([int(x) for x in words])
+
+
+@pytest.mark.parametrize("name,pfx", [("fr_ops", "fr"), ("fq_ops", "fq")])
+def test_golden_field_vectors(dev, name, pfx):
+    """the committed field vectors (shapes of bend2/tests/test_fr.bend, test_fq.bend) through the
+    device arithmetic: a, b, a + b, a - b, a b, -a, 1/a, a^2, canonical a"""
+    rec = _records(("vectors", name + ".bin"), 9 * 16).reshape(-1, 9, 16)
+    W = dev.words
+    for r in rec:
+        a, b = _v16(r[0]), _v16(r[1])
+        assert dev.call(pfx + "_add", [W(a), W(b)], 8) == _v16(r[2])
+        assert dev.call(pfx + "_sub", [W(a), W(b)], 8) == _v16(r[3])
+        assert dev.call(pfx + "_mul", [W(a), W(b)], 8) == _v16(r[4])
+        assert dev.call(pfx + "_neg", [W(a)], 8) == _v16(r[5])
+        assert dev.call(pfx + "_inv", [W(a)], 8) == _v16(r[6])
+        assert dev.call(pfx + "_sqr", [W(a)], 8) == _v16(r[7])
+        assert dev.call(pfx + "_from_mont", [W(a)], 8) == _v16(r[8])
+        if pfx == "fq":
+            assert dev.call("fq_fmul", [W(a), W(b)], 8) == _v16(r[4])
+            assert dev.call("fq_fsqr", [W(a)], 8) == _v16(r[7])
+
+
+def test_golden_montmul_pairs(dev):
+    """the 1000 Montgomery products from the reference's check_montmul.py operand generator"""
+    rec = _records(("montmul_fr.bin",), 3 * 16).reshape(-1, 3, 16)
+    W = dev.words
+    for r in rec:
+        assert dev.call("fr_mul", [W(_v16(r[0])), W(_v16(r[1]))], 8) == _v16(r[2])
+
+
+@pytest.mark.parametrize("name,g2", [("g1_ops", False), ("g2_ops", True)], ids=["g1", "g2"])
+def test_golden_curve_vectors(dev, name, g2):
+    """the committed curve vectors (shapes of bend2/tests/test_g1.bend, test_g2.bend; cases 0-2
+    are infinity, P = Q and P = -Q): P + Q by the mixed addition and 2P by the XYZZ doubling of
+    the device, normalised to affine on the host"""
+    pw = 64 if g2 else 32
+    rec = _records(("vectors", name + ".bin"), 6 * pw + 16)
+    curve = o.G2 if g2 else o.G1
+    io = CurveIO(dev, curve, g2)
+    fe = 16  # wire words per Fq element
+
+    def aff(words):
+        vals = [o.from_mont(_v16(words[i * fe:(i + 1) * fe]), PQ) for i in range(pw // fe)]
+        if not any(vals):
+            return None
+        return ((vals[0], vals[1]), (vals[2], vals[3])) if g2 else (vals[0], vals[1])
+
+    pfx = "g2" if g2 else "g1"
+    nw = 4 * io.fw
+    for r in rec:
+        P, Q = aff(r[0:pw]), aff(r[pw:2 * pw])
+        want_add, want_dbl = aff(r[2 * pw + 16:3 * pw + 16]), aff(r[3 * pw + 16:4 * pw + 16])
+        xp = dev.call(pfx + "_from_affine", [io.affine(P)], nw)
+        got = io.from_xyzz(dev.call(pfx + "_madd", [dev.words(xp, nw), io.affine(Q)], nw))
+        assert got == want_add
+        assert io.from_xyzz(dev.call(pfx + "_dbl", [dev.words(xp, nw)], nw)) == want_dbl
