@@ -57,12 +57,27 @@ int guard(bg_ctx* ctx, Fn&& fn) {
     return e.status;
   } catch (const std::bad_alloc&) {
     if (ctx) ctx->c.last_error = "host allocation failed";
+    else g_err_noctx = "host allocation failed";
     return BG_E_OOM;
   } catch (const std::exception& e) {
     if (ctx) ctx->c.last_error = e.what();
+    else g_err_noctx = e.what();
     return BG_E_DEVICE;
   }
 }
+
+// a failed argument check of an entry point: BG_E_ARG, with the failed condition in the message
+int arg_error(bg_ctx* ctx, const char* fn, const char* condition) {
+  const std::string m = std::string(fn) + ": invalid argument (" + condition + ")";
+  if (ctx) ctx->c.last_error = m;
+  else g_err_noctx = m;
+  return BG_E_ARG;
+}
+
+#define BG_ARG_CHECK(ctx, bad)                              \
+  do {                                                      \
+    if (bad) return arg_error((ctx), __func__, #bad);       \
+  } while (0)
 
 void require(bool ok, const char* msg) {
   if (!ok) throw Error(BG_E_ARG, msg);
@@ -219,7 +234,7 @@ bool read_file(const std::string& path, std::vector<char>& out) {
 extern "C" {
 
 int bg_ctx_create(int device, bg_ctx** out) {
-  if (!out) return BG_E_ARG;
+  BG_ARG_CHECK(nullptr, !out);
   *out = nullptr;
   bg_ctx* ctx = new bg_ctx();
   int st = guard(nullptr, [&] { ctx_init(ctx->c, device); });
@@ -266,7 +281,7 @@ void* bg_ctx_stream(bg_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; 
 uint64_t bg_ctx_launches(const bg_ctx*) { return g_launches.load(); }
 
 int bg_host_alloc(size_t bytes, void** out) {
-  if (!out) return BG_E_ARG;
+  BG_ARG_CHECK(nullptr, !out);
   cudaError_t e = cudaMallocHost(out, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -285,15 +300,14 @@ int bg_msm_table_window_bits(size_t n, int curve) { return msm_pick_c_table(n, c
 int bg_msm_proof_window_bits(size_t n, int curve) { return msm_pick_c_proof(n, curve == BG_CURVE_G2); }
 
 int bg_msm_window_override(bg_ctx* ctx, int layout, int curve, int c) {
-  if (!ctx || (layout != 0 && layout != 1) || (curve != BG_CURVE_G1 && curve != BG_CURVE_G2) ||
-      (c != 0 && (c < 2 || c > 22)))
-    return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || (layout != 0 && layout != 1) || (curve != BG_CURVE_G1 && curve != BG_CURVE_G2) ||
+                        (c != 0 && (c < 2 || c > 22)));
   ctx->c.c_override[layout][curve == BG_CURVE_G2 ? 1 : 0] = c;
   return BG_OK;
 }
 
 int bg_msm_g1(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, size_t n, uint32_t* out_jac16) {
-  if (!ctx || !out_jac16 || (n && (!points16 || !scalars16))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !out_jac16 || (n && (!points16 || !scalars16)));
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     msm_host<Fq, bgh::FqOps>(ctx->c, points16, scalars16, n, out_jac16);
@@ -301,7 +315,7 @@ int bg_msm_g1(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, 
 }
 
 int bg_msm_g2(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, size_t n, uint32_t* out_jac16) {
-  if (!ctx || !out_jac16 || (n && (!points16 || !scalars16))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !out_jac16 || (n && (!points16 || !scalars16)));
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     msm_host<Fq2, bgh::Fq2Ops>(ctx->c, points16, scalars16, n, out_jac16);
@@ -309,7 +323,7 @@ int bg_msm_g2(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, 
 }
 
 int bg_msm_g1_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32) {
-  if (!ctx || !out_aff32 || (n && (!d_points || !d_scalars))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !out_aff32 || (n && (!d_points || !d_scalars)));
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     msm_dev<Fq>(ctx->c, d_points, d_scalars, n, out_aff32);
@@ -317,7 +331,7 @@ int bg_msm_g1_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scala
 }
 
 int bg_msm_g2_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32) {
-  if (!ctx || !out_aff32 || (n && (!d_points || !d_scalars))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !out_aff32 || (n && (!d_points || !d_scalars)));
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     msm_dev<Fq2>(ctx->c, d_points, d_scalars, n, out_aff32);
@@ -326,7 +340,7 @@ int bg_msm_g2_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scala
 
 int bg_qap_h(bg_ctx* ctx, const uint32_t* a16, const uint32_t* b16, const uint32_t* c16, uint32_t log2d,
              uint32_t* h16) {
-  if (!ctx || !a16 || !b16 || !c16 || !h16 || log2d > 27) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !a16 || !b16 || !c16 || !h16 || log2d > 27);
   return guard(ctx, [&] {
     Ctx& c = ctx->c;
     cudaSetDevice(c.device);
@@ -346,7 +360,7 @@ int bg_qap_h(bg_ctx* ctx, const uint32_t* a16, const uint32_t* b16, const uint32
 }
 
 int bg_ntt(bg_ctx* ctx, uint32_t* data16, uint32_t log2n, int mode) {
-  if (!ctx || !data16 || log2n > 27 || mode < 0 || mode > 3) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !data16 || log2n > 27 || mode < 0 || mode > 3);
   return guard(ctx, [&] {
     Ctx& c = ctx->c;
     cudaSetDevice(c.device);
@@ -360,7 +374,7 @@ int bg_ntt(bg_ctx* ctx, uint32_t* data16, uint32_t log2n, int mode) {
 }
 
 int bg_ntt_dev(bg_ctx* ctx, uint32_t* d_data, uint32_t log2n, int mode) {
-  if (!ctx || !d_data || log2n > 27 || mode < 0 || mode > 3) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !d_data || log2n > 27 || mode < 0 || mode > 3);
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     ntt_run(ctx->c, ctx->c.stream, d_data, (int)log2n, mode);
@@ -368,20 +382,20 @@ int bg_ntt_dev(bg_ctx* ctx, uint32_t* d_data, uint32_t log2n, int mode) {
 }
 
 int bg_repack_to_packed_dev(bg_ctx* ctx, const uint32_t* d_wire, uint32_t* d_packed, size_t n) {
-  if (!ctx || (n && (!d_wire || !d_packed))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || (n && (!d_wire || !d_packed)));
   return guard(ctx, [&] { wire_to_packed(ctx->c.stream, d_wire, d_packed, n, ctx->c.d_status); });
 }
 
 int bg_repack_to_wire_dev(bg_ctx* ctx, const uint32_t* d_packed, uint32_t* d_wire, size_t n) {
-  if (!ctx || (n && (!d_wire || !d_packed))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || (n && (!d_wire || !d_packed)));
   return guard(ctx, [&] { packed_to_wire(ctx->c.stream, d_packed, d_wire, n); });
 }
 
 int bg_field_op(bg_ctx* ctx, int field, int op, const uint32_t* a16, const uint32_t* b16, uint32_t* out16,
                 size_t n) {
   const bool binary = op == BG_FOP_ADD || op == BG_FOP_SUB || op == BG_FOP_MUL;
-  if (!ctx || (field != BG_FIELD_FR && field != BG_FIELD_FQ) || op < 0 || op > BG_FOP_FROM_MONT) return BG_E_ARG;
-  if (n && (!a16 || !out16 || (binary && !b16))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || (field != BG_FIELD_FR && field != BG_FIELD_FQ) || op < 0 || op > BG_FOP_FROM_MONT);
+  BG_ARG_CHECK(ctx, n && (!a16 || !out16 || (binary && !b16)));
   return guard(ctx, [&] {
     Ctx& c = ctx->c;
     cudaSetDevice(c.device);
@@ -398,8 +412,8 @@ int bg_field_op(bg_ctx* ctx, int field, int op, const uint32_t* a16, const uint3
 
 int bg_curve_op(bg_ctx* ctx, int curve, int op, const uint32_t* p16, const uint32_t* q16, const uint32_t* k16,
                 uint32_t* out16, size_t n) {
-  if (!ctx || (curve != BG_CURVE_G1 && curve != BG_CURVE_G2) || op < 0 || op > BG_COP_MUL) return BG_E_ARG;
-  if (n && (!p16 || !out16 || (op == BG_COP_ADD && !q16) || (op == BG_COP_MUL && !k16))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || (curve != BG_CURVE_G1 && curve != BG_CURVE_G2) || op < 0 || op > BG_COP_MUL);
+  BG_ARG_CHECK(ctx, n && (!p16 || !out16 || (op == BG_COP_ADD && !q16) || (op == BG_COP_MUL && !k16)));
   return guard(ctx, [&] {
     Ctx& c = ctx->c;
     cudaSetDevice(c.device);
@@ -417,7 +431,7 @@ int bg_curve_op(bg_ctx* ctx, int curve, int op, const uint32_t* p16, const uint3
 }
 
 int bg_pk_upload(bg_ctx* ctx, const bg_inputs* in, bg_pk** out) {
-  if (!ctx || !in || !out) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !in || !out);
   *out = nullptr;
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
@@ -436,7 +450,7 @@ void bg_pk_release(bg_pk* pk) {
 
 int bg_prove_resident(bg_ctx* ctx, bg_pk* pk, const uint32_t* witness16, const uint32_t* rs16, bg_proof* out,
                       bg_phase_ms* times) {
-  if (!ctx || !pk || !witness16 || !rs16 || !out) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !pk || !witness16 || !rs16 || !out);
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     prove_resident(ctx->c, *pk->pk, witness16, rs16, out, times, 0.0);
@@ -445,10 +459,9 @@ int bg_prove_resident(bg_ctx* ctx, bg_pk* pk, const uint32_t* witness16, const u
 
 int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnesses, const uint32_t* const* rs,
                    size_t count, int lanes, bg_proof* out, bg_phase_ms* times, int* statuses) {
-  if (!ctx || (count && (!pks || !witnesses || !rs || !out || !statuses)) || lanes < 1 || lanes > 32)
-    return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || (count && (!pks || !witnesses || !rs || !out || !statuses)) || lanes < 1 || lanes > 32);
   for (size_t i = 0; i < count; i++)
-    if (!pks[i] || !witnesses[i] || !rs[i] || pks[i]->owner != ctx) return BG_E_ARG;
+    BG_ARG_CHECK(ctx, !pks[i] || !witnesses[i] || !rs[i] || pks[i]->owner != ctx);
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     while ((int)ctx->lanes.size() < lanes) {
@@ -489,7 +502,7 @@ int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnes
 size_t bg_prove_footprint(const bg_pk* pk) { return pk ? prove_footprint(pk->pk->h) : 0; }
 
 int bg_server_create(bg_ctx* ctx, int lanes, size_t hbm_budget_bytes, bg_server** out) {
-  if (!ctx || !out || lanes < 1 || lanes > 32 || hbm_budget_bytes == 0) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !out || lanes < 1 || lanes > 32 || hbm_budget_bytes == 0);
   *out = nullptr;
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
@@ -498,13 +511,13 @@ int bg_server_create(bg_ctx* ctx, int lanes, size_t hbm_budget_bytes, bg_server*
 }
 
 int bg_server_submit(bg_server* s, bg_pk* pk, const uint32_t* witness16, const uint32_t* rs16, uint64_t tag) {
-  if (!s || !pk || !witness16 || !rs16 || pk->owner != s->owner) return BG_E_ARG;
+  BG_ARG_CHECK(s ? s->owner : nullptr, !s || !pk || !witness16 || !rs16 || pk->owner != s->owner);
   return guard(s->owner, [&] { server_submit(s->s, pk->pk, witness16, rs16, tag); });
 }
 
 int bg_server_wait(bg_server* s, int timeout_ms, uint64_t* tag, bg_proof* out, bg_phase_ms* times,
                    double* latency_ms, double* queue_ms, int* status) {
-  if (!s || !tag || !status || timeout_ms < 0) return BG_E_ARG;
+  BG_ARG_CHECK(s ? s->owner : nullptr, !s || !tag || !status || timeout_ms < 0);
   return server_wait(s->s, timeout_ms, tag, out, times, latency_ms, queue_ms, status) ? BG_OK : BG_E_TIMEOUT;
 }
 
@@ -517,7 +530,7 @@ void bg_server_destroy(bg_server* s) {
 }
 
 int bg_prove_host(bg_ctx* ctx, const bg_inputs* in, bg_proof* out, bg_phase_ms* times) {
-  if (!ctx || !in || !out) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !in || !out);
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     const auto t0 = std::chrono::steady_clock::now();
@@ -537,7 +550,7 @@ int bg_prove_host(bg_ctx* ctx, const bg_inputs* in, bg_proof* out, bg_phase_ms* 
 }
 
 int bg_prove_dir(bg_ctx* ctx, const char* dir, bg_proof* out, bg_phase_ms* times) {
-  if (!ctx || !dir || !out) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !dir || !out);
   return guard(ctx, [&] {
     const auto t0 = std::chrono::steady_clock::now();
     static const char* names[13] = {"header", "witness", "r1cs_a", "r1cs_b", "r1cs_c", "pk_g1", "pk_g2",
@@ -575,7 +588,7 @@ int bg_prove_dir(bg_ctx* ctx, const char* dir, bg_proof* out, bg_phase_ms* times
 }
 
 int bg_synth_square_chain(bg_ctx* ctx, uint32_t log2n, uint64_t seed, const char* dir) {
-  if (!ctx || !dir) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !dir);
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     synth_square_chain(ctx->c, log2n, seed, dir);
@@ -583,7 +596,7 @@ int bg_synth_square_chain(bg_ctx* ctx, uint32_t log2n, uint64_t seed, const char
 }
 
 int bg_ctx_profile(bg_ctx* ctx, int enable) {
-  if (!ctx) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx);
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
     for (int i = 0; i < kStreams; i++) BG_CUDA(cudaStreamSynchronize(ctx->c.side[i]));
@@ -599,7 +612,7 @@ int bg_ctx_profile(bg_ctx* ctx, int enable) {
 }
 
 int bg_ctx_timeline(bg_ctx* ctx, int enable, char* buf, size_t cap) {
-  if (!ctx || (!enable && (!buf || cap == 0))) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || (!enable && (!buf || cap == 0)));
   return guard(ctx, [&] {
     Ctx& c = ctx->c;
     cudaSetDevice(c.device);
@@ -630,7 +643,7 @@ int bg_ctx_timeline(bg_ctx* ctx, int enable, char* buf, size_t cap) {
 }
 
 int bg_ctx_transfer_bytes(bg_ctx* ctx, uint64_t* h2d, uint64_t* d2h) {
-  if (!ctx || !h2d || !d2h) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !h2d || !d2h);
   return guard(ctx, [&] {
     *h2d = ctx->c.h2d_bytes;
     *d2h = ctx->c.d2h_bytes;
@@ -642,7 +655,7 @@ int bg_ctx_transfer_bytes(bg_ctx* ctx, uint64_t* h2d, uint64_t* d2h) {
 }
 
 int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms) {
-  if (!ctx || !name || !launches || !total_ms) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !name || !launches || !total_ms);
   return guard(ctx, [&] {
     *launches = 0;
     *total_ms = 0;
@@ -664,7 +677,7 @@ int bg_ctx_kernel_stats(bg_ctx* ctx, const char* name, uint64_t* launches, doubl
 }
 
 int bg_probe_imad(bg_ctx* ctx, int which, uint32_t iters, double* ops, double* ms) {
-  if (!ctx || !ops || !ms || which < 0 || which > 4 || iters == 0) return BG_E_ARG;
+  BG_ARG_CHECK(ctx, !ctx || !ops || !ms || which < 0 || which > 4 || iters == 0);
   return guard(ctx, [&] {
     Ctx& c = ctx->c;
     cudaSetDevice(c.device);
@@ -689,12 +702,12 @@ int bg_probe_imad(bg_ctx* ctx, int which, uint32_t iters, double* ops, double* m
 }
 
 int bg_proof_format(const bg_proof* proof, char* buf, size_t buf_bytes) {
-  if (!proof || !buf) return BG_E_ARG;
+  BG_ARG_CHECK(nullptr, !proof || !buf);
   return format_proof(proof, buf, buf_bytes);
 }
 
 int bg_verify(const bg_vk* vk, const uint32_t* public16, size_t n_public, const bg_proof* proof, int* valid) {
-  if (!vk || !proof || !valid) return BG_E_ARG;
+  BG_ARG_CHECK(nullptr, !vk || !proof || !valid);
   try {
     const bgh::VkWire w{vk->alpha_g1, vk->beta_g2, vk->gamma_g2, vk->delta_g2, vk->gamma_abc_g1, vk->n_ic};
     *valid = bgh::groth16_verify(w, public16, n_public, proof->a, proof->b, proof->c);
@@ -706,7 +719,7 @@ int bg_verify(const bg_vk* vk, const uint32_t* public16, size_t n_public, const 
 }
 
 int bg_pairing(const uint32_t* p32, const uint32_t* q64, uint32_t* out192) {
-  if (!p32 || !q64 || !out192) return BG_E_ARG;
+  BG_ARG_CHECK(nullptr, !p32 || !q64 || !out192);
   try {
     bgh::pairing_wire(p32, q64, out192);
     return BG_OK;

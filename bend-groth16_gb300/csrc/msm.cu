@@ -1067,7 +1067,10 @@ void msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t 
 
 extern "C" int bg_msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t n, void* stream,
                                  uint32_t* out_aff32) {
-  if (!out_aff32 || (n && (!d_points || !d_scalars))) return BG_E_ARG;
+  if (!out_aff32 || (n && (!d_points || !d_scalars))) {
+    bg::set_noctx_error("bg_msm_g1_noalloc: invalid argument (a null pointer)");
+    return BG_E_ARG;
+  }
   std::lock_guard<std::mutex> lock(bg::g_noalloc_mu);
   try {
     bg::msm_g1_noalloc(d_points, d_scalars, n, static_cast<cudaStream_t>(stream), out_aff32);

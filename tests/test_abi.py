@@ -3,6 +3,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from conftest import ROOT
 
 
@@ -31,3 +33,33 @@ def test_status_strings(built_lib):
     assert L.bg_msm_window_bits(1 << 20, 0) >= L.bg_msm_window_bits(1 << 10, 0)
     assert L.bg_msm_table_window_bits(1 << 18, 1) >= L.bg_msm_table_window_bits(1 << 10, 1)
     assert 3 <= L.bg_msm_proof_window_bits(1 << 18, 1) <= 20
+
+
+def test_argument_errors_carry_a_message(built_lib):
+    """a rejected argument returns BG_E_ARG and bg_last_error names the entry point and the
+    failed condition; these checks run before any device work, so no GPU is needed"""
+    import bendg
+    L = bendg.lib()
+    out = (ctypes.c_uint32 * 48)()
+    assert L.bg_msm_g1(None, None, None, 4, out) == bendg.BG_E_ARG
+    msg = L.bg_last_error(None).decode()
+    assert msg.startswith("bg_msm_g1: invalid argument") and "!ctx" in msg
+    assert L.bg_qap_h(None, None, None, None, 30, None) == bendg.BG_E_ARG
+    assert L.bg_last_error(None).decode().startswith("bg_qap_h: invalid argument")
+    assert L.bg_msm_g1_noalloc(None, None, 4, None, out) == bendg.BG_E_ARG
+    assert L.bg_last_error(None).decode().startswith("bg_msm_g1_noalloc: invalid argument")
+    assert L.bg_proof_format(None, None, 0) == bendg.BG_E_ARG
+    assert L.bg_last_error(None).decode().startswith("bg_proof_format: invalid argument")
+
+
+def test_no_device_fails_loudly(built_lib):
+    """without a usable GPU, creating a context fails with BG_E_DEVICE and the CUDA reason:
+    there is no CPU fallback behind the C ABI"""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import bendg
+    with pytest.raises(bendg.BgError) as e:
+        bendg.Context(0)
+    assert e.value.status == bendg.BG_E_DEVICE
+    assert "bg_ctx_create" in str(e.value) or "cuda" in str(e.value).lower()
