@@ -638,7 +638,8 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
                        "unit": "Gimad/s", "frac": round(achieved / (imad_peak / 1e9), 4), "traffic": traffic,
                        "work_per_launch": work, "avg_launch_ms": round(avg, 4), "launches": launches,
                        "peak_source": "bg_probe_imad on this GPU (32-bit mad.lo/mad.hi chains)",
-                       "work_model": "n W entries x %d IMAD per mixed add (c=%d, W=%d)" % (MADD_G1_IMAD, c, W)}
+                       "work_model": "n W entries x %d IMAD per mixed add (c=%d, W=%d)" % (MADD_G1_IMAD, c, W),
+                       "hbm": acc_hbm_view(n1, c, W, avg, traffic)}
     if only_g1:
         return res
     n2 = 1 << 18
@@ -650,6 +651,24 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
     res["coset_ntt_2^20_ms"] = timeit(lambda: ctx.ntt_dev(x.data_ptr(), 20, 2) or torch.cuda.synchronize())
     res["ntt_roofline"] = ntt_roofline(20, res["ntt_2^20_forward_ms"], imad_peak)
     return res
+
+
+def acc_hbm_view(n, c, W, avg_ms, traffic=None):
+    """the G1 accumulation kernel against the HBM roofline: its minimal bytes per launch are
+    the n affine points read once (64 B each), the n W entry codes read (4 B each) and the W
+    2^(c-1) XYZZ buckets written (128 B each); the slice pieces of cut buckets come on top, so
+    this is a lower bound.  The kernel is bound by its multiply-adds, so the fraction is small."""
+    hbm_gbs = None
+    pf = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pf):
+        hbm_gbs = json.load(open(pf)).get("hbm_gbs")
+    min_bytes = n * 64 + n * W * 4 + W * (1 << (c - 1)) * 128
+    achieved = min_bytes / (avg_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_gbs, "unit": "GB/s",
+            "frac": round(achieved / hbm_gbs, 4) if hbm_gbs else None, "traffic": traffic,
+            "algorithmic_bytes": min_bytes,
+            "model": "points n x 64 B + entry codes n W x 4 B + buckets W 2^(c-1) x 128 B (lower bound)",
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
 
 
 def ntt_roofline(lg, ms, imad_peak):
