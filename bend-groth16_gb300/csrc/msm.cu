@@ -892,11 +892,50 @@ void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32) {
     for (uint32_t m = plan.part_span; m > 1; m >>= 1) jr = bgh::xyzz_dbl(jr);
     wsum[w] = bgh::xyzz_add(s, jr);
   };
+  // One window of many parts (the shared bucket set of a key's window tables, e.g. J = 128 for
+  // msm_h of a SquareChain(2^18) proof: ~390 host additions after the proof's last kernel) is
+  // split into power-of-two chunks of parts on the host pool.  Chunk c covers parts [lo, lo + C)
+  // with lo = c C and gives s_c = sum S_j, t_c = sum R_j, u_c = sum (j - lo) R_j; then
+  // sum_j j R_j = sum_c u_c + C sum_{c>=1} c t_c, the last sum by a running sum over chunks.
+  auto single_window_chunked = [&]() {
+    const uint32_t J = plan.J;
+    const uint32_t chunks = std::min<uint32_t>(16, J / 8), C = J / chunks;
+    const uint32_t* pw = plan.host_window_sums;
+    std::vector<bgh::Xyzz<H>> cs(chunks), ct(chunks), cu(chunks);
+    HostPool::get().parallel_for((int)chunks, [&](int c) {
+      const uint32_t lo = (uint32_t)c * C;
+      bgh::Xyzz<H> s = bgh::xyzz_inf<H>(), run = bgh::xyzz_inf<H>(), u = bgh::xyzz_inf<H>();
+      for (int j = (int)(lo + C) - 1; j >= (int)lo; j--) {
+        s = bgh::xyzz_add(s, bgh::xyzz_from_words32<H>(pw + (size_t)(2 * j) * PW));
+        run = bgh::xyzz_add(run, bgh::xyzz_from_words32<H>(pw + (size_t)(2 * j + 1) * PW));
+        if (j > (int)lo) u = bgh::xyzz_add(u, run);
+      }
+      cs[c] = s;
+      ct[c] = run;
+      cu[c] = u;
+    });
+    bgh::Xyzz<H> s = bgh::xyzz_inf<H>(), jr = bgh::xyzz_inf<H>(), run = bgh::xyzz_inf<H>(),
+                 ctop = bgh::xyzz_inf<H>();
+    for (int c = (int)chunks - 1; c >= 0; c--) {
+      s = bgh::xyzz_add(s, cs[c]);
+      jr = bgh::xyzz_add(jr, cu[c]);
+      if (c >= 1) {
+        run = bgh::xyzz_add(run, ct[c]);
+        ctop = bgh::xyzz_add(ctop, run);  // sum_{c>=1} c t_c
+      }
+    }
+    for (uint32_t m = C; m > 1; m >>= 1) ctop = bgh::xyzz_dbl(ctop);
+    jr = bgh::xyzz_add(jr, ctop);  // sum_{j>=1} j R_j
+    for (uint32_t m = plan.part_span; m > 1; m >>= 1) jr = bgh::xyzz_dbl(jr);
+    wsum[0] = bgh::xyzz_add(s, jr);
+  };
   // The window sums of a bucket-set-per-window MSM are about two thirds of its host work
   // (17 windows x 8 parts: ~550 of ~850 point operations); they run on the host pool, the
   // Horner chain after them stays serial.  SquareChain(2^18) one-shot proof: the G2 finish is
   // the tail of the proof.
-  if (plan.W >= 4 && (size_t)plan.W * plan.J >= 32) HostPool::get().parallel_for(plan.W, window_sum);
+  const bool pow2_parts = plan.J >= 32 && (plan.J & (plan.J - 1)) == 0;
+  if (plan.W == 1 && pow2_parts && HostPool::get().workers() > 0) single_window_chunked();
+  else if (plan.W >= 4 && (size_t)plan.W * plan.J >= 32) HostPool::get().parallel_for(plan.W, window_sum);
   else
     for (int w = 0; w < plan.W; w++) window_sum(w);
   bgh::Xyzz<H> acc = bgh::xyzz_inf<H>();

@@ -564,6 +564,9 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   msm_finish<Fq2>(plan[2], res[2]);
   const Xyzz<Fq2Ops> B2 = bgh::xyzz_add(
       bgh::xyzz_add(bgh::xyzz_from(bgh::aff_from_words32<Fq2Ops>(res[2])), s_delta2), bgh::xyzz_from(pk.beta2));
+  // A and B are final here: their inversions to affine run while msm_h is still on the device
+  const auto a_aff = bgh::xyzz_to_affine(A);
+  const auto b_aff = bgh::xyzz_to_affine(B2);
   drain(plan[4]);
   msm_finish<Fq>(plan[4], res[4]);
   c_part = bgh::xyzz_add(c_part, g1(res[4]));
@@ -572,8 +575,8 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   check_status(ctx, st);
   msm_finish<Fq>(plan[3], res[3]);
   const Xyzz<FqOps> C = bgh::xyzz_add(c_part, g1(res[3]));
-  wire_from_affine<FqOps>(out->a, bgh::xyzz_to_affine(A));
-  wire_from_affine<Fq2Ops>(out->b, bgh::xyzz_to_affine(B2));
+  wire_from_affine<FqOps>(out->a, a_aff);
+  wire_from_affine<Fq2Ops>(out->b, b_aff);
   wire_from_affine<FqOps>(out->c, bgh::xyzz_to_affine(C));
 
   if (times) {
