@@ -305,6 +305,43 @@ def build(out_dir: str | None = None) -> str:
     return so
 
 
+_DIGITS_EXPORTS = r"""
+extern "C" {
+int digit_window_width(int w, int W) { return bg::window_width(w, W); }
+int digit_window_offset(int w, int W) { return bg::window_offset(w, W); }
+/* signed digits of one scalar (8 limbs) over W windows, as k_digits_hist and k_scatter make
+ * them; returns the carry left after the top window */
+uint32_t digits(const uint32_t* s, int W, uint32_t* mags, uint8_t* negs) {
+  uint32_t carry = 0;
+  for (int w = 0; w < W; w++) {
+    bool ng = false;
+    mags[w] = bg::signed_digit(s, w, W, carry, ng);
+    negs[w] = ng ? 1 : 0;
+  }
+  return carry;
+}
+}
+"""
+
+
+def build_digits(out_dir: str) -> str:
+    """the MSM's window layout and signed-digit recoding (the digits section of msm.cu, from
+    window_bits to signed_digit, which k_digits_hist and k_scatter call) compiled for the host;
+    returns the shared library's path"""
+    src_text = open(os.path.join(CSRC, "msm.cu")).read()
+    start = src_text.index("BG_DEV uint32_t window_bits(")
+    end = src_text.index("__global__ void k_digits_hist(")
+    section = src_text[start:end]
+    os.makedirs(out_dir, exist_ok=True)
+    src = os.path.join(out_dir, "digits_emul.cpp")
+    with open(src, "w") as f:
+        f.write(_PRELUDE + "#define BG_DEV inline\n#define __host__\n#define __device__\n#define __restrict__\n"
+                + "namespace bg {\n" + section + "}  // namespace bg\n" + _DIGITS_EXPORTS)
+    so = os.path.join(out_dir, "libdigits_emul.so")
+    subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-w", "-o", so, src], check=True)
+    return so
+
+
 class DeviceArith:
     """ctypes view of the compiled emulation; values are Python ints, Montgomery form where
     the device keeps them so (the caller converts)"""

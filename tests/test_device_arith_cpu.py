@@ -5,7 +5,8 @@ squaring products over the whole 256-bit operand range; the Montgomery reduction
 input range [0, p R); the lazy-reduction forms a b - c d; Fq2 (bend2/src/fq2.bend:31-50); the
 XYZZ formulas of G1 and G2 with every special case (infinity on either side, P = Q, P = -Q).
 The committed golden vectors (field ops, the 1000 Montgomery pairs, G1/G2 ops) go through the
-same emulated functions.  Every asm statement must also set the carry flag before reading it.
+same emulated functions, and the MSM's window layout and signed-digit recoding (msm.cu) are
+checked for every window width.  Every asm statement must also set the carry flag before reading it.
 No GPU is involved."""
 import random
 
@@ -321,3 +322,48 @@ def test_golden_curve_vectors(dev, name, g2):
         got = io.from_xyzz(dev.call(pfx + "_madd", [dev.words(xp, nw), io.affine(Q)], nw))
         assert got == want_add
         assert io.from_xyzz(dev.call(pfx + "_dbl", [dev.words(xp, nw)], nw)) == want_dbl
+
+
+@pytest.fixture(scope="module")
+def digits_lib(tmp_path_factory):
+    import ctypes
+    return ctypes.CDLL(device_emul.build_digits(str(tmp_path_factory.mktemp("digits_emul"))))
+
+
+def test_msm_window_layout_and_signed_digits(digits_lib):
+    """the MSM's balanced windows and signed-digit recoding (msm.cu, used by k_digits_hist and
+    k_scatter) for every window width the library accepts: the W = floor(254 / c) + 1 windows
+    tile bits [0, 255) with widths of at most c, every digit's magnitude is at most 2^(b-1) for
+    its b-bit window (so its bucket index fits 2^(c-1) buckets), no carry leaves the top window,
+    and sum_w +-|d_w| 2^(o_w) gives the scalar back -- for edge scalars (0, 1, r - 1, 2^254 - 1,
+    all-ones and alternating bit patterns, runs that make carries ripple) and random ones"""
+    import ctypes
+    L = digits_lib
+    L.digits.restype = ctypes.c_uint32
+    rng = random.Random(20)
+    top = (1 << 254) - 1
+    edge = [0, 1, 2, PR - 1, top, top // 3, (top // 3) * 2, (1 << 253), (1 << 253) - 1]
+    edge += [((1 << k) - 1) for k in (15, 16, 17, 31, 32, 33, 127, 128, 200, 253)]
+    for c in range(2, 23):
+        W = 254 // c + 1
+        widths = [L.digit_window_width(w, W) for w in range(W)]
+        offsets = [L.digit_window_offset(w, W) for w in range(W)]
+        assert sum(widths) == 255 and max(widths) <= c and min(widths) >= max(widths) - 1
+        assert offsets == [sum(widths[:w]) for w in range(W)]
+        # scalars whose every window digit sits at the sign boundary 2^(b-1) and just above it
+        half = sum(1 << (o + b - 1) for o, b in zip(offsets, widths)) & top
+        above = sum(((1 << (b - 1)) + 1) << o for o, b in zip(offsets, widths)) & top
+        cases = edge + [half, above] + [rng.getrandbits(254) for _ in range(300 if c < 8 else 60)]
+        mags = (ctypes.c_uint32 * W)()
+        negs = (ctypes.c_uint8 * W)()
+        for s in cases:
+            words = (ctypes.c_uint32 * 8)(*[(s >> (32 * i)) & 0xFFFFFFFF for i in range(8)])
+            carry = L.digits(words, W, mags, negs)
+            assert carry == 0, (c, s)
+            total = 0
+            for w in range(W):
+                assert mags[w] <= 1 << (widths[w] - 1), (c, s, w)
+                # a window of all ones plus a carry gives magnitude 0 (flagged negative, with
+                # the carry passed up): no bucket entry, as the kernels skip magnitude 0
+                total += (-1 if negs[w] else 1) * mags[w] << offsets[w]
+            assert total == s, (c, s)
