@@ -14,8 +14,11 @@ PTX semantics emulated (PTX ISA, integer arithmetic instructions, extended preci
 `.u32`.  `.cc` writes the carry flag (a borrow for `sub`/`subc`), `addc`/`subc`/`madc` read
 it.  The flag starts undefined in every asm statement, as it does on the device (the compiler
 may clobber it between statements): an instruction that reads it before one in the same
-statement wrote it records a fault, which the tests assert never happens.  Any other opcode,
-type or operand constraint makes the translation fail loudly.
+statement wrote it records a fault, which the tests assert never happens.  Likewise a
+write-only output (`=r`) or a scratch register declared in the statement must be written before
+it is read, and every `=r` output must be written; the translation checks this (each asm
+statement is straight-line code) and fails otherwise.  Any other opcode, type or operand
+constraint makes the translation fail loudly too.
 """
 import ctypes
 import os
@@ -99,7 +102,10 @@ def _operand_expr(tok: str, names: set) -> str:
     raise ValueError("unknown PTX operand %r" % tok)
 
 
-def _instruction(line: str, names: set) -> str:
+def _instruction(line: str, names: set, unset: set) -> str:
+    """C++ for one PTX instruction; `unset` holds the operands that have no value yet (write-only
+    outputs and scratch registers not written so far in this statement): reading one is an
+    error, writing one removes it"""
     op, _, rest = line.strip().partition(" ")
     m = _OPCODE.match(op)
     if not m:
@@ -109,6 +115,10 @@ def _instruction(line: str, names: set) -> str:
     need = {"mul": 3, "mad": 4, "madc": 4}.get(base, 3)
     if len(args) != need:
         raise ValueError("wrong operand count in %r" % line)
+    for src in args[1:]:
+        if src in unset:
+            raise ValueError("%r reads an operand that has no value yet" % line)
+    unset.discard(args[0])
     if base in ("mul", "mad", "madc") and not half:
         raise ValueError("mul/mad without .lo/.hi: %r" % line)
     d, a, b = args[0], args[1], args[2]
@@ -150,10 +160,13 @@ def translate_asm(body: str) -> str:
         raise ValueError("asm clobbers are not expected: %r" % parts[3])
     ops = outs + ins
     code = ["{ int _cf = 2;"]
+    unset = set()
     for k, (cons, expr) in enumerate(ops):
         if k < len(outs):
             if cons not in ("=r", "+r"):
                 raise ValueError("output constraint %r not emulated" % cons)
+            if cons == "=r":
+                unset.add("_o%d" % k)
             code.append("uint32_t _o%d%s;" % (k, " = (uint32_t)(%s)" % expr if cons == "+r" else ""))
         else:
             if cons not in ("r", "n"):
@@ -171,9 +184,13 @@ def translate_asm(body: str) -> str:
             for nm in m.group(1).split(","):
                 nm = nm.strip()
                 names.add(nm)
+                unset.add("_v_" + nm)
                 code.append("uint32_t _v_%s = 0;" % nm)
             continue
-        code.append(_instruction(stmt, names))
+        code.append(_instruction(stmt, names, unset))
+    never = sorted(u for u in unset if u.startswith("_o"))
+    if never:
+        raise ValueError("asm outputs never written: %s" % ", ".join(never))
     for k, (cons, expr) in enumerate(outs):
         code.append("(%s) = _o%d;" % (expr, k))
     code.append("(void)_cf; }")

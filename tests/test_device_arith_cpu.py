@@ -367,3 +367,14 @@ def test_msm_window_layout_and_signed_digits(digits_lib):
                 # the carry passed up): no bucket entry, as the kernels skip magnitude 0
                 total += (-1 if negs[w] else 1) * mags[w] << offsets[w]
             assert total == s, (c, s)
+
+
+def test_emulation_rejects_a_read_of_an_unwritten_output(tmp_path):
+    """a chain that reads one of its own write-only outputs before writing it (undefined on the
+    device) is refused when the headers are translated"""
+    def edit(src):
+        t = (src / "fp.cuh").read_text()
+        i = t.index('asm("add.cc.u32  %0, %8,', t.index("BG_DEV Fp<P> add("))
+        (src / "fp.cuh").write_text(t[:i] + 'asm("add.cc.u32  %0, %1,' + t[i + len('asm("add.cc.u32  %0, %8,'):])
+    with pytest.raises(ValueError, match="no value yet"):
+        _mutated_build(tmp_path, edit)
