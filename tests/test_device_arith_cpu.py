@@ -201,6 +201,9 @@ def test_xyzz_formulas(dev, g2):
             assert got == want, (pfx, "madd", i, A is None, B is None)
             got = io.from_xyzz(dev.call(pfx + "_add", [io.xyzz(A, lp), io.xyzz(B, lq)], nw))
             assert got == want, (pfx, "add", i, A is None, B is None)
+            # commuted (the reference's commuted-add case, bend2/tests/test_g1.bend)
+            got = io.from_xyzz(dev.call(pfx + "_madd", [io.xyzz(B, lq), io.affine(A)], nw))
+            assert got == want, (pfx, "madd commuted", i, A is None, B is None)
         assert io.from_xyzz(dev.call(pfx + "_dbl", [io.xyzz(P, lp)], nw)) == curve.double(P)
         assert io.from_xyzz(dev.call(pfx + "_dbl", [io.xyzz(None, lp)], nw)) is None
         assert io.from_xyzz(dev.call(pfx + "_dbl_affine", [io.affine(P)], nw)) == curve.double(P)

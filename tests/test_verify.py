@@ -89,6 +89,13 @@ def test_verify_golden_proofs(built_lib, k):
     off = golden_proof(k)
     np.ctypeslib.as_array(off.c)[16] ^= 1  # C off the curve
     assert not bendg.verify(*vk, pub, off)
+    # the rejections of ref/src/verify.rs:35-51: C at infinity, A off the curve
+    c_inf = golden_proof(k)
+    np.ctypeslib.as_array(c_inf.c)[:] = 0
+    assert not bendg.verify(*vk, pub, c_inf)
+    a_off = golden_proof(k)
+    np.ctypeslib.as_array(a_off.a)[0] ^= 1
+    assert not bendg.verify(*vk, pub, a_off)
 
 
 def test_verify_rejects_wrong_public_count(built_lib):
