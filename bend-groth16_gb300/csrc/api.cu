@@ -712,6 +712,10 @@ int bg_verify(const bg_vk* vk, const uint32_t* public16, size_t n_public, const 
     const bgh::VkWire w{vk->alpha_g1, vk->beta_g2, vk->gamma_g2, vk->delta_g2, vk->gamma_abc_g1, vk->n_ic};
     *valid = bgh::groth16_verify(w, public16, n_public, proof->a, proof->b, proof->c);
     return BG_OK;
+  } catch (const bgh::MalformedInput& e) {
+    *valid = 0;
+    bg::set_noctx_error(e.what());
+    return BG_E_FORMAT;
   } catch (const std::exception& e) {
     bg::set_noctx_error(e.what());
     return BG_E_ARG;

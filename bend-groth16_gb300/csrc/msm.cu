@@ -946,14 +946,21 @@ void msm_finish(const MsmPlan& plan, uint32_t* out_affine_words32) {
   bgh::aff_to_words32<H>(out_affine_words32, bgh::xyzz_to_affine(acc));
 }
 
+// Kernel attributes (the opt-in to large dynamic shared memory) apply to the device that is
+// current when they are set, so they are set once per device; batch lanes and server threads
+// may get here at the same time, hence the per-device once flags.
+constexpr int kInitMaxDevices = 64;
 void msm_init_kernels() {
-  static bool done = false;
-  if (done) return;
+  static std::once_flag once[kInitMaxDevices];
   static_assert(!kReduceInSmem<Fq> && kReduceInSmem<Fq2>, "reduction forms: G1 in registers, G2 in shared memory");
-  BG_CUDA(cudaFuncSetAttribute(k_window_reduce<Fq>, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 32 * 4));
-  BG_CUDA(cudaFuncSetAttribute(k_window_reduce_sm<Fq2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)reduce_sm_bytes<Fq2>(256)));
-  done = true;
+  int dev = 0;
+  BG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kInitMaxDevices) throw Error(BG_E_ARG, "msm: device index out of range");
+  std::call_once(once[dev], [] {
+    BG_CUDA(cudaFuncSetAttribute(k_window_reduce<Fq>, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 32 * 4));
+    BG_CUDA(cudaFuncSetAttribute(k_window_reduce_sm<Fq2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)reduce_sm_bytes<Fq2>(256)));
+  });
 }
 
 template void msm_launch<Fq>(Ctx&, cudaStream_t, const std::string&, const uint32_t*, const uint32_t*, size_t,
@@ -987,7 +994,9 @@ template void msm_finish<Fq2>(const MsmPlan&, uint32_t*);
 //     this entry point serialises calls made from one process and returns only when its work
 //     is complete;
 //   * the first call on a device looks up the array's device address on that device (the
-//     device current at the call); make that first call before any stream capture.
+//     device current at the call);
+//   * every call ends with a synchronisation of its stream and copies to pageable host memory,
+//     so it must not be called on a stream that is being captured.
 namespace bg {
 namespace {
 
@@ -1118,5 +1127,11 @@ extern "C" int bg_msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_sca
     bg::set_noctx_error(e.what());
     if (e.status == BG_E_DEVICE) cudaGetLastError();
     return e.status;
+  } catch (const std::bad_alloc&) {
+    bg::set_noctx_error("bg_msm_g1_noalloc: host allocation failed");
+    return BG_E_OOM;
+  } catch (const std::exception& e) {
+    bg::set_noctx_error(std::string("bg_msm_g1_noalloc: ") + e.what());
+    return BG_E_DEVICE;
   }
 }

@@ -326,25 +326,25 @@ int groth16_verify(const VkWire& vk, const uint32_t* public16, size_t n_public, 
   if (!limbs_ok(vk.alpha_g1, 32) || !limbs_ok(vk.beta_g2, 64) || !limbs_ok(vk.gamma_g2, 64) ||
       !limbs_ok(vk.delta_g2, 64) || !limbs_ok(vk.gamma_abc_g1, 32 * vk.n_ic) || !limbs_ok(a32, 32) ||
       !limbs_ok(b64, 64) || !limbs_ok(c32, 32) || (n_public && !limbs_ok(public16, 16 * n_public)))
-    return 0;
+    throw MalformedInput("bg_verify: a wire word has bits above its 16-bit limb");
   const G1A alpha = g1_from_wire(vk.alpha_g1), A = g1_from_wire(a32), Cp = g1_from_wire(c32);
   const G2A beta = g2_from_wire(vk.beta_g2), gamma = g2_from_wire(vk.gamma_g2), delta = g2_from_wire(vk.delta_g2);
   const G2A B = g2_from_wire(b64);
   if (!g1_valid(alpha) || !g1_valid(A) || !g1_valid(Cp) || !g2_valid(beta) || !g2_valid(gamma) ||
       !g2_valid(delta) || !g2_valid(B))
-    return 0;
+    throw MalformedInput("bg_verify: a proof or key point is off its curve or outside the order-r subgroup");
   // vk_x = IC_0 + sum_i x_i IC_{i+1}
   Xyzz<FqOps> acc = xyzz_inf<FqOps>();
   for (size_t i = 0; i < vk.n_ic; i++) {
     const G1A ic = g1_from_wire(vk.gamma_abc_g1 + 32 * i);
-    if (!g1_valid(ic)) return 0;
+    if (!g1_valid(ic)) throw MalformedInput("bg_verify: an IC point is off the curve");
     const Aff<FqOps> p{ic.x, ic.y, ic.inf};
     if (i == 0) {
       acc = xyzz_add(acc, xyzz_from(p));
       continue;
     }
     const Fe xm = fe_from_words16(public16 + 16 * (i - 1));
-    if (!below(xm, FR)) return 0;
+    if (!below(xm, FR)) throw MalformedInput("bg_verify: a public input is not below r");
     const Fe x = fe_from_mont(FR, xm);
     acc = xyzz_add(acc, xyzz_mul(xyzz_from(p), x.v));
   }

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <stdexcept>
 
 namespace bgh {
 
@@ -16,10 +17,17 @@ struct VkWire {
   size_t n_ic;                   // public inputs + 1
 };
 
+// A point off its curve or outside the order-r subgroup, a wire word above 16 bits or a public
+// input not below r: an input that cannot be decoded, which the reference's verifier reports as
+// an error rather than a rejection (ref/src/verify.rs:9-26, its test at :47-49).
+struct MalformedInput : std::invalid_argument {
+  using std::invalid_argument::invalid_argument;
+};
+
 // 1: e(A, B) = e(alpha, beta) e(sum_i x_i IC_i, gamma) e(C, delta) with x_0 = 1 and
-// x_1.. = public16 (n_ic - 1 Fr elements, wire layout, Montgomery); 0: the equation fails or a
-// point is off its curve / outside the order-r subgroup.  Throws std::invalid_argument on
-// malformed sizes.
+// x_1.. = public16 (n_ic - 1 Fr elements, wire layout, Montgomery); 0: the equation fails.
+// Throws MalformedInput for undecodable points or inputs, std::invalid_argument on malformed
+// sizes.
 int groth16_verify(const VkWire& vk, const uint32_t* public16, size_t n_public, const uint32_t* a32,
                    const uint32_t* b64, const uint32_t* c32);
 

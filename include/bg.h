@@ -163,7 +163,10 @@ typedef struct bg_vk {
   size_t n_ic;
 } bg_vk;
 /* *valid = 1 when e(A, B) = e(alpha, beta) e(vk_x, gamma) e(C, delta), vk_x = IC_0 +
- * sum_i x_i IC_i, with every point on its curve and B in the order-r subgroup; 0 otherwise.
+ * sum_i x_i IC_i; 0 when the equation fails (a wrong proof of valid points, C at infinity
+ * included).  Inputs that cannot be decoded -- a point off its curve or B outside the order-r
+ * subgroup, a wire word above 16 bits, a public input not below r -- return BG_E_FORMAT with
+ * *valid = 0, as the reference's verifier errors on them (ref/src/verify.rs:9-26, :47-49).
  * public16: n_public Fr elements (wire layout, Montgomery; x_1.. of z), n_public = n_ic - 1
  * (BG_E_ARG otherwise).  Host only (optimal ate pairing on the CPU, a few ms); needs no
  * context or GPU. */
@@ -202,7 +205,8 @@ int bg_msm_g2_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scala
  * share the array (each clears what must start at zero); calls from one process are
  * serialised and the function returns when its work is done, and calls that overlapped on the
  * GPU would race.  The first call on a device looks up the array's address on the current
- * device; make it before any stream capture.  Errors: bg_last_error(NULL). */
+ * device.  Every call synchronises `stream` and copies to pageable host memory, so it must not
+ * be called while that stream is being captured.  Errors: bg_last_error(NULL). */
 int bg_msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_scalars, size_t n, void* stream,
                       uint32_t* out_aff32);
 int bg_ntt_dev(bg_ctx* ctx, uint32_t* d_data, uint32_t log2n, int mode);

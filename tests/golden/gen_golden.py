@@ -12,7 +12,8 @@ encoding (ref/README.md:13-22) and then pushed through the reference's OWN tooli
   * bend2/probe/check_montmul.py deterministic Montgomery pairs  (pins a*b*R^-1 mod p)
 The oracle's own qap_h must agree with ref_qap.py's h bit for bit before anything is written.
 
-Usage: python tests/golden/gen_golden.py [REFERENCE_ROOT]   (default: /root/reference)
+Usage: python tests/golden/gen_golden.py REFERENCE_ROOT
+       (or set BEND_GROTH16_REF to the checkout's root and give no argument)
 """
 from __future__ import annotations
 
@@ -236,7 +237,12 @@ def proof_lines(proof) -> str:
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BEND_GROTH16_REF")
+    if not root:
+        sys.exit("usage: gen_golden.py REFERENCE_ROOT (or set BEND_GROTH16_REF): the bend-groth16 checkout")
+    ref = Path(root)
+    if not (ref / "bend2" / "FORMAT.md").is_file():
+        sys.exit("%s does not hold a bend-groth16 checkout (no bend2/FORMAT.md)" % ref)
     export_bin = load_ref_module(ref, "bend2/tools/export_bin.py", "ref_export_bin")
     verify_bin = load_ref_module(ref, "bend2/tools/verify_bin.py", "ref_verify_bin")
     ref_qap = load_ref_module(ref, "bend2/gen/ref_qap.py", "ref_ref_qap")

@@ -86,16 +86,23 @@ def test_verify_golden_proofs(built_lib, k):
     np.ctypeslib.as_array(swapped.a)[:] = np.ctypeslib.as_array(swapped.c)
     np.ctypeslib.as_array(swapped.c)[:] = a
     assert not bendg.verify(*vk, pub, swapped)
-    off = golden_proof(k)
-    np.ctypeslib.as_array(off.c)[16] ^= 1  # C off the curve
-    assert not bendg.verify(*vk, pub, off)
-    # the rejections of ref/src/verify.rs:35-51: C at infinity, A off the curve
+    # the cases of ref/src/verify.rs:35-51: C at infinity is a valid point and a rejected proof;
+    # A (or C) off the curve cannot be decoded and is an error, not a rejection
     c_inf = golden_proof(k)
     np.ctypeslib.as_array(c_inf.c)[:] = 0
     assert not bendg.verify(*vk, pub, c_inf)
-    a_off = golden_proof(k)
-    np.ctypeslib.as_array(a_off.a)[0] ^= 1
-    assert not bendg.verify(*vk, pub, a_off)
+    for field, word in (("a", 0), ("c", 16)):
+        off = golden_proof(k)
+        np.ctypeslib.as_array(getattr(off, field))[word] ^= 1
+        with pytest.raises(bendg.BgError) as err:
+            bendg.verify(*vk, pub, off)
+        assert err.value.status == bendg.BG_E_FORMAT
+    # a public input not below r is undecodable too
+    big = np.concatenate([wire(o.fe_bytes_mont(0, o.P_FR)) for _ in pub_hex])
+    big[:16] = 0xFFFF
+    with pytest.raises(bendg.BgError) as err:
+        bendg.verify(*vk, big, proof)
+    assert err.value.status == bendg.BG_E_FORMAT
 
 
 def test_verify_rejects_wrong_public_count(built_lib):

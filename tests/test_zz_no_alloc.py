@@ -50,6 +50,35 @@ def test_noalloc_matches_allocating_msm(ctx):
                 np.stack([got & 0xffff, got >> 16], axis=1).reshape(-1)))
             assert (x, y) == o.FixedBase(o.G1, o.G1.gen).mul(sum(a * b for a, b in zip(ks, sc)) % o.P_FR)
 
+    # small n take the fallback width rule (narrow windows, many of them), where the layout's
+    # guards are tightest; n = 0 gives infinity (all zero) like the allocating path
+    for n in (1, 8, 200, 1000, 0):
+        sc = [int.from_bytes(rng.bytes(32), "little") % o.P_FR for _ in range(max(n, 1))]
+        d_sc = torch.from_numpy(packed(scalars_wire(sc)).view(np.int32)).cuda()
+        torch.cuda.synchronize()
+        want = ctx.msm_g1_dev(d_pts.data_ptr(), d_sc.data_ptr(), n)
+        got = np.full(16, 0xdead, dtype=np.uint32)
+        st = L.bg_msm_g1_noalloc(d_pts.data_ptr(), d_sc.data_ptr(), n, None, got.ctypes.data_as(ctypes.c_void_p))
+        assert st == bendg.BG_OK, L.bg_last_error(None)
+        assert np.array_equal(got, want), n
+
+    # a scalar not below 2^254 is rejected, and the next valid call is unaffected
+    n = 200
+    sc = [int.from_bytes(rng.bytes(32), "little") % o.P_FR for _ in range(n)]
+    bad = packed(scalars_wire(sc))
+    bad[8 * 17 + 7] |= 0xC0000000
+    d_bad = torch.from_numpy(bad.view(np.int32)).cuda()
+    torch.cuda.synchronize()
+    got = np.zeros(16, dtype=np.uint32)
+    st = L.bg_msm_g1_noalloc(d_pts.data_ptr(), d_bad.data_ptr(), n, None, got.ctypes.data_as(ctypes.c_void_p))
+    assert st == bendg.BG_E_ARG and b"2^254" in L.bg_last_error(None)
+    d_sc = torch.from_numpy(packed(scalars_wire(sc)).view(np.int32)).cuda()
+    torch.cuda.synchronize()
+    want = ctx.msm_g1_dev(d_pts.data_ptr(), d_sc.data_ptr(), n)
+    st = L.bg_msm_g1_noalloc(d_pts.data_ptr(), d_sc.data_ptr(), n, None, got.ctypes.data_as(ctypes.c_void_p))
+    assert st == bendg.BG_OK, L.bg_last_error(None)
+    assert np.array_equal(got, want)
+
     too_many = np.zeros(16, dtype=np.uint32)
     st = L.bg_msm_g1_noalloc(d_pts.data_ptr(), d_pts.data_ptr(), MAX_POINTS + 1, None,
                              too_many.ctypes.data_as(ctypes.c_void_p))
