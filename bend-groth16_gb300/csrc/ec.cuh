@@ -46,6 +46,13 @@ BG_DEV Fq2 field_inv_any(const Fq2& a) {
   return {fmul(a.c0, ni), neg(fmul(a.c1, ni))};
 }
 
+// 1/a by binary Euclid (fp.cuh): the latency-critical single inversion of a batch
+BG_DEV Fq field_inv_fast(const Fq& a) { return inv_binary(a); }
+BG_DEV Fq2 field_inv_fast(const Fq2& a) {
+  const Fq ni = inv_binary(add(fsqr(a.c0), fsqr(a.c1)));
+  return {fmul(a.c0, ni), neg(fmul(a.c1, ni))};
+}
+
 template <class F>
 struct Affine {
   F x, y;
@@ -184,6 +191,53 @@ BG_DEV XYZZ<F> xyzz_add(const XYZZ<F>& p, const XYZZ<F>& q) {
   r.y = fmul_sub(r_, sub(qq, r.x), s1, ppp);
   r.zz = fmul(zz12, pp);
   r.zzz = fmul(zzz12, ppp);
+  return r;
+}
+
+// ---------------------------------------------------------------- affine pair additions
+// P + Q for affine P and Q where the caller supplies 1/d for the denominator d: the
+// batch-affine accumulation inverts the denominators of many additions at once (Montgomery's
+// simultaneous inversion), so an addition costs the chord slope and the new coordinates
+// (two products and a square) plus its three products of the shared inversion, against
+// madd-2008-s's eight products and two squares.  pair_kind picks the case and its denominator:
+// the chord (x_Q - x_P), the tangent (2 y_P) when P = Q, or none (a result of infinity, or one
+// input at infinity).  The affine infinity is (0, 0) as everywhere on the device.
+enum : uint32_t { kPairChord = 0, kPairTangent = 1, kPairInf = 2, kPairFirst = 3, kPairSecond = 4 };
+
+template <class F>
+BG_DEV uint32_t pair_kind(const Affine<F>& p, const Affine<F>& q, F& d) {
+  if (is_inf(p)) return kPairSecond;
+  if (is_inf(q)) return kPairFirst;
+  d = sub(q.x, p.x);
+  if (!is_zero(d)) return kPairChord;
+  if (eq(p.y, q.y) && !is_zero(p.y)) {
+    d = dbl(p.y);
+    return kPairTangent;
+  }
+  return kPairInf;  // Q = -P (or a point of order two, which the prime-order groups lack)
+}
+
+// the sum for the case pair_kind chose; dinv = 1 / d for the chord and tangent cases
+template <class F>
+BG_DEV Affine<F> pair_finish(const Affine<F>& p, const Affine<F>& q, uint32_t kind, const F& dinv) {
+  if (kind == kPairFirst) return p;
+  if (kind == kPairSecond) return q;
+  Affine<F> r;
+  if (kind == kPairInf) {
+    r.x = field_zero<F>();
+    r.y = field_zero<F>();
+    return r;
+  }
+  F num;
+  if (kind == kPairChord) {
+    num = sub(q.y, p.y);
+  } else {
+    const F x2 = fsqr(p.x);
+    num = add(dbl(x2), x2);
+  }
+  const F l = fmul(num, dinv);
+  r.x = sub(sub(fsqr(l), p.x), q.x);  // the tangent case has q.x = p.x
+  r.y = sub(fmul(l, sub(p.x, r.x)), p.y);
   return r;
 }
 

@@ -28,6 +28,9 @@ struct FqParams {
   // R mod p (Montgomery one)
   static constexpr uint32_t ONE0 = 0xc58f0d9du, ONE1 = 0xd35d438du, ONE2 = 0xf5c70b3du, ONE3 = 0x0a78eb28u,
                             ONE4 = 0x7879462cu, ONE5 = 0x666ea36fu, ONE6 = 0x9a07df2fu, ONE7 = 0x0e0a77c1u;
+  // R^3 mod p (turns the inverse of a Montgomery representative into a Montgomery inverse)
+  static constexpr uint32_t R3_0 = 0xda1530dfu, R3_1 = 0xb1cd6dafu, R3_2 = 0xa7283db6u, R3_3 = 0x62f210e6u,
+                            R3_4 = 0x0ada0afbu, R3_5 = 0xef7f0b0cu, R3_6 = 0x2d592544u, R3_7 = 0x20fd6e90u;
 };
 struct FrParams {
   static constexpr uint32_t P0 = 0xf0000001u, P1 = 0x43e1f593u, P2 = 0x79b97091u, P3 = 0x2833e848u,
@@ -35,6 +38,8 @@ struct FrParams {
   static constexpr uint32_t N0 = 0xefffffffu;
   static constexpr uint32_t ONE0 = 0x4ffffffbu, ONE1 = 0xac96341cu, ONE2 = 0x9f60cd29u, ONE3 = 0x36fc7695u,
                             ONE4 = 0x7879462eu, ONE5 = 0x666ea36fu, ONE6 = 0x9a07df2fu, ONE7 = 0x0e0a77c1u;
+  static constexpr uint32_t R3_0 = 0xb4bf0040u, R3_1 = 0x5e94d8e1u, R3_2 = 0x1cfbb6b8u, R3_3 = 0x2a489cbeu,
+                            R3_4 = 0xa19fcfedu, R3_5 = 0x893cc664u, R3_6 = 0x7fcc657cu, R3_7 = 0x0cf8594bu;
 };
 
 template <class P>
@@ -255,6 +260,145 @@ template <class P>
 BG_DEV Fp<P> inv(const Fp<P>& a) {
   const uint32_t e[8] = {P::P0 - 2u, P::P1, P::P2, P::P3, P::P4, P::P5, P::P6, P::P7};
   return pow_limbs(a, e);
+}
+
+// ---------------------------------------------------------------- inversion by binary Euclid
+// 1/a for a Montgomery element a (0 -> 0).  Binary extended Euclid (Hankerson, Menezes and
+// Vanstone, Guide to Elliptic Curve Cryptography, Algorithm 2.22) on the representative aR,
+// with the invariants (aR) x1 = u and (aR) x2 = v (mod p) from u = aR, v = p: strip the factors
+// of two from u (x1 follows with x1 / 2^k mod p), subtract the smaller of the odd u, v from the
+// larger (x1 or x2 follows), until u or v is 1; one Montgomery product by R^3 mod p then turns
+// (aR)^-1 into a^-1 R.  The k trailing zeros of u leave in one step: x1 / 2^k mod p is the exact
+// quotient (x1 + m p) / 2^k with m = x1 (-p^-1) mod 2^k, which is below p for x1 < p, so a
+// pass is a subtraction, a shift and one 8-limb multiply-add, about 250 passes in all.  One
+// thread computes the inversion that a whole CTA of the batch-affine bucket accumulation waits
+// for, so its latency is what counts (the Fermat power is 320 dependent products).  Variable
+// time (the inputs are public bucket coordinates).  Requires a < p (every stored element is).
+namespace binv {
+BG_DEV bool is_one8(const uint32_t* u) {
+  return u[0] == 1u && (u[1] | u[2] | u[3] | u[4] | u[5] | u[6] | u[7]) == 0u;
+}
+BG_DEV int ctz32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+  return __ffs((int)x) - 1;
+#else
+  return __builtin_ctz(x);
+#endif
+}
+// u >>= k, 1 <= k <= 31
+BG_DEV void shr8(uint32_t* u, int k) {
+#pragma unroll
+  for (int i = 0; i < 7; i++) u[i] = (u[i] >> k) | (u[i + 1] << (32 - k));
+  u[7] >>= k;
+}
+// x = x / 2^k mod p for x < p, 1 <= k <= 31: (x + m p) / 2^k, m = x n0' mod 2^k
+BG_DEV void div2k_mod(uint32_t* x, int k, const uint32_t* p, uint32_t n0) {
+  const uint32_t m = (x[0] * n0) & ((1u << k) - 1u);
+  uint32_t t[9];
+  uint64_t c = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    c += (uint64_t)x[i] + (uint64_t)m * p[i];
+    t[i] = (uint32_t)c;
+    c >>= 32;
+  }
+  t[8] = (uint32_t)c;
+#pragma unroll
+  for (int i = 0; i < 8; i++) x[i] = (t[i] >> k) | (t[i + 1] << (32 - k));
+}
+// strip the factors of two of u (u != 0), dividing x by the same power of two mod p
+BG_DEV void strip2(uint32_t* u, uint32_t* x, const uint32_t* p, uint32_t n0) {
+  for (int limb = 0; limb < 8 && u[0] == 0u; limb++) {  // rare: a whole zero limb, two steps of 16 bits
+#pragma unroll
+    for (int i = 0; i < 7; i++) u[i] = u[i + 1];
+    u[7] = 0u;
+    div2k_mod(x, 16, p, n0);
+    div2k_mod(x, 16, p, n0);
+  }
+  if (u[0] == 0u) return;  // u = 0: only for an input that is 0 mod p
+  const int k = ctz32(u[0]);
+  if (k) {
+    shr8(u, k);
+    div2k_mod(x, k, p, n0);
+  }
+}
+// u -= v when u >= v (returns true), else leaves u and returns false
+BG_DEV bool sub_if_geq(uint32_t* u, const uint32_t* v) {
+  uint32_t d[8];
+  uint64_t b = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const uint64_t t = (uint64_t)u[i] - v[i] - b;
+    d[i] = (uint32_t)t;
+    b = t >> 63;
+  }
+  if (b) return false;
+#pragma unroll
+  for (int i = 0; i < 8; i++) u[i] = d[i];
+  return true;
+}
+BG_DEV void sub8(uint32_t* u, const uint32_t* v) {
+  uint64_t b = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const uint64_t t = (uint64_t)u[i] - v[i] - b;
+    u[i] = (uint32_t)t;
+    b = t >> 63;
+  }
+}
+// x = x - y mod p (x, y < p)
+BG_DEV void sub_mod(uint32_t* x, const uint32_t* y, const uint32_t* p) {
+  uint64_t b = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const uint64_t t = (uint64_t)x[i] - y[i] - b;
+    x[i] = (uint32_t)t;
+    b = t >> 63;
+  }
+  if (b) {
+    uint64_t c = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      c += (uint64_t)x[i] + p[i];
+      x[i] = (uint32_t)c;
+      c >>= 32;
+    }
+  }
+}
+}  // namespace binv
+
+template <class P>
+BG_DEV Fp<P> inv_binary(const Fp<P>& a) {
+  if (is_zero(a)) return a;
+  const uint32_t p[8] = {P::P0, P::P1, P::P2, P::P3, P::P4, P::P5, P::P6, P::P7};
+  uint32_t u[8], v[8], x1[8], x2[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    u[i] = a.v[i];
+    v[i] = p[i];
+    x1[i] = 0;
+    x2[i] = 0;
+  }
+  x1[0] = 1;
+  // v is odd from the start and after every strip; each pass removes at least one bit from
+  // u v (below 2^508), so 512 passes always suffice
+  for (int pass = 0; pass < 512; pass++) {
+    binv::strip2(u, x1, p, P::N0);
+    if (binv::is_one8(u) || binv::is_one8(v)) break;
+    if (binv::sub_if_geq(u, v)) {
+      binv::sub_mod(x1, x2, p);
+    } else {
+      binv::sub8(v, u);
+      binv::sub_mod(x2, x1, p);
+      binv::strip2(v, x2, p, P::N0);
+    }
+  }
+  Fp<P> r, r3;
+#pragma unroll
+  for (int i = 0; i < 8; i++) r.v[i] = binv::is_one8(u) ? x1[i] : x2[i];
+  r3.v[0] = P::R3_0; r3.v[1] = P::R3_1; r3.v[2] = P::R3_2; r3.v[3] = P::R3_3;
+  r3.v[4] = P::R3_4; r3.v[5] = P::R3_5; r3.v[6] = P::R3_6; r3.v[7] = P::R3_7;
+  return mul(r, r3);
 }
 
 // ---------------------------------------------------------------- Fq2 = Fq[u]/(u^2 + 1)

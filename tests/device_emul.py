@@ -253,6 +253,18 @@ template <class F> static void stx(uint32_t* d, const XYZZ<F>& p) {
 template <class F> static Affine<F> lda(const uint32_t* s) {
   constexpr int W = FieldWords<F>::value; Affine<F> p; ldf(p.x, s); ldf(p.y, s + W); return p;
 }
+template <class F> static void sta(uint32_t* d, const Affine<F>& p) {
+  constexpr int W = FieldWords<F>::value; stf(d, p.x); stf(d + W, p.y);
+}
+/* one affine pair addition as the batch-affine rounds make it, with a one-element batch: the
+ * denominator pair_kind picks, inverted by the binary-Euclid inverse, into pair_finish */
+template <class F> static void pair_add_impl(const uint32_t* p, const uint32_t* q, uint32_t* r, uint32_t* kind) {
+  const Affine<F> P = lda<F>(p), Q = lda<F>(q);
+  F d = field_zero<F>();
+  *kind = pair_kind(P, Q, d);
+  const F dinv = *kind <= kPairTangent ? field_inv_fast(d) : field_zero<F>();
+  sta(r, pair_finish(P, Q, *kind, dinv));
+}
 
 #define FIELD_OPS(PFX, PARAMS)                                                                  \
   void PFX##_add(const uint32_t* a, const uint32_t* b, uint32_t* r) { st(r, add(ld<PARAMS>(a), ld<PARAMS>(b))); } \
@@ -261,6 +273,7 @@ template <class F> static Affine<F> lda(const uint32_t* s) {
   void PFX##_mul(const uint32_t* a, const uint32_t* b, uint32_t* r) { st(r, mul(ld<PARAMS>(a), ld<PARAMS>(b))); } \
   void PFX##_sqr(const uint32_t* a, uint32_t* r) { st(r, sqr(ld<PARAMS>(a))); }                 \
   void PFX##_inv(const uint32_t* a, uint32_t* r) { st(r, inv(ld<PARAMS>(a))); }                 \
+  void PFX##_inv_binary(const uint32_t* a, uint32_t* r) { st(r, inv_binary(ld<PARAMS>(a))); }   \
   void PFX##_from_mont(const uint32_t* a, uint32_t* r) { st(r, from_mont(ld<PARAMS>(a))); }     \
   void PFX##_redc(const uint32_t* t16, uint32_t* r) { Wide t; memcpy(t.v, t16, 64); st(r, redc<PARAMS>(t)); }
 
@@ -284,6 +297,9 @@ void fq2_fmul_sub(const uint32_t* a, const uint32_t* b, const uint32_t* c, const
   st2(r, fmul_sub(ld2(a), ld2(b), ld2(c), ld2(d)));
 }
 void fq2_inv(const uint32_t* a, uint32_t* r) { st2(r, field_inv_any(ld2(a))); }
+void fq2_inv_fast(const uint32_t* a, uint32_t* r) { st2(r, field_inv_fast(ld2(a))); }
+void g1_pair_add(const uint32_t* p, const uint32_t* q, uint32_t* kind, uint32_t* r) { pair_add_impl<Fq>(p, q, r, kind); }
+void g2_pair_add(const uint32_t* p, const uint32_t* q, uint32_t* kind, uint32_t* r) { pair_add_impl<Fq2>(p, q, r, kind); }
 
 #define CURVE_OPS(PFX, F)                                                                       \
   void PFX##_madd(const uint32_t* p, const uint32_t* q, uint32_t* r) { stx(r, xyzz_madd(ldx<F>(p), lda<F>(q))); } \

@@ -56,6 +56,20 @@ def test_field_ops(dev, pfx, p, rinv):
         assert dev.call(pfx + "_inv", [W(a)], 8) == want
 
 
+@pytest.mark.parametrize("pfx,p,rinv", [("fq", PQ, RINV_Q), ("fr", PR, RINV_R)])
+def test_binary_euclid_inverse(dev, pfx, p, rinv):
+    """inv_binary (the single inversion of a batch-affine round) is the Montgomery inverse on
+    edge operands (small values, powers of two -- the longest runs of halvings -- values next to
+    p and to the Montgomery one) and on random ones; inv(0) = 0"""
+    W = dev.words
+    rng = random.Random(21)
+    vals = edges(p) + [1 << k for k in range(0, 254, 7)] + [p - (1 << k) for k in range(1, 250, 13)]
+    vals += [o.R256 % p + 1, (o.R256 * o.R256) % p] + [rng.randrange(p) for _ in range(400)]
+    for a in vals:
+        want = 0 if a == 0 else pow(a * rinv, -1, p) * o.R256 % p
+        assert dev.call(pfx + "_inv_binary", [W(a)], 8) == want, hex(a)
+
+
 def test_wide_products_full_range(dev):
     """the 512-bit products are exact for any 256-bit operands (the Fq2 Karatsuba sums reach 2p)"""
     W = dev.words
@@ -118,6 +132,9 @@ def test_fq2(dev):
         if i % 10 == 0:
             want = (0, 0) if a == (0, 0) else o.f2_inv(a)
             assert f2_value(dev.call("fq2_inv", [A], 16)) == want
+        if i % 3 == 0:
+            want = (0, 0) if a == (0, 0) else o.f2_inv(a)
+            assert f2_value(dev.call("fq2_inv_fast", [A], 16)) == want
 
 
 class CurveIO:
@@ -209,6 +226,38 @@ def test_xyzz_formulas(dev, g2):
         assert io.from_xyzz(dev.call(pfx + "_dbl_affine", [io.affine(P)], nw)) == curve.double(P)
         assert io.from_xyzz(dev.call(pfx + "_from_affine", [io.affine(P)], nw)) == P
         assert io.from_xyzz(dev.call(pfx + "_from_affine", [io.affine(None)], nw)) is None
+
+
+@pytest.mark.parametrize("g2", [False, True], ids=["g1", "g2"])
+def test_affine_pair_additions(dev, g2):
+    """the affine pair addition of the batch-affine rounds (pair_kind + pair_finish) with every
+    case: the chord, the tangent (P = Q), P = -Q, infinity on either side or both"""
+    import ctypes
+    curve = o.G2 if g2 else o.G1
+    io = CurveIO(dev, curve, g2)
+    pfx = "g2" if g2 else "g1"
+    rng = random.Random(22 + g2)
+    f = o.FixedBase(curve, curve.gen)
+    pts = [f.mul(rng.randrange(1, PR)) for _ in range(10 if g2 else 30)]
+    nw = 2 * io.fw
+    bits = 32 * io.fw
+
+    def add(A, B):
+        kind = ctypes.c_uint32()
+        out = (ctypes.c_uint32 * nw)()
+        getattr(dev.lib, pfx + "_pair_add")(io.affine(A), io.affine(B), ctypes.byref(kind), out)
+        v = dev.value(out)
+        x, y = io.fe_value(v & ((1 << bits) - 1)), io.fe_value(v >> bits)
+        zero = (0, 0) if g2 else 0
+        return kind.value, (None if (x, y) == (zero, zero) else (x, y))
+
+    for i, P in enumerate(pts):
+        Q = pts[(i + 1) % len(pts)]
+        for A, B, k in [(P, Q, 0), (P, P, 1), (P, curve.neg(P), 2), (P, None, 3), (None, Q, 4), (None, None, 4)]:
+            kind, got = add(A, B)
+            assert kind == k and got == curve.add(A, B), (pfx, i, k)
+            if got is not None:
+                assert curve.on_curve(got)
 
 
 def _mutated_build(tmp_path, edit):
