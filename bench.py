@@ -47,8 +47,51 @@ REF_GPU_K18_MS = 56083.0
 # 2 x 464 + 848 = 5136.
 MADD_G1_IMAD = 6 * (96 + 136) + 2 * (72 + 136) + (2 * 96 + 136)
 MADD_G2_IMAD = 6 * (3 * 96 + 2 * 136) + 2 * 2 * (96 + 136) + (6 * 96 + 2 * 136)
-KERNEL_FAMILIES = ["msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_heavy_g1", "msm_heavy_g2", "msm_reduce_g1",
-                   "msm_reduce_g2", "msm_digits", "msm_scatter", "ntt_pass"]
+# per affine pair addition of the batch-affine rounds (msm_pairs.cuh): three products of the
+# shared inversion (running product, 1/d, and the inverse walked back), the slope, its square
+# and y3: 5 products + 1 square.  G1: 5 x 232 + 208 = 1368; G2: 5 x 560 + 464 = 3264.
+PAIR_G1_IMAD = 5 * (96 + 136) + (72 + 136)
+PAIR_G2_IMAD = 5 * (3 * 96 + 2 * 136) + 2 * (96 + 136)
+KERNEL_FAMILIES = ["msm_pair_g1", "msm_pair_g2", "msm_bucket_acc_g1", "msm_bucket_acc_g2", "msm_heavy_g1",
+                   "msm_heavy_g2", "msm_reduce_g1", "msm_reduce_g2", "msm_digits", "msm_scatter", "ntt_pass"]
+
+
+def bucket_counts(sc_u32, c: int):
+    """entries per bucket key of one bucket set per window, for (n, 8) uint32 canonical scalars
+    and window width c: the balanced window layout and signed digits of msm.cu (window_width,
+    window_offset, signed_digit), key = w 2^(c-1) + |d| - 1"""
+    import numpy as np
+    W = 254 // c + 1
+    nb = 1 << (c - 1)
+    base, extra = 255 // W, 255 % W
+    limbs = sc_u32.astype(np.uint64)
+    carry = np.zeros(sc_u32.shape[0], dtype=np.uint64)
+    counts = np.zeros(W * nb, dtype=np.int64)
+    for w in range(W):
+        b = base + (1 if w < extra else 0)
+        off = w * base + min(w, extra)
+        li, sh = off // 32, off % 32
+        v = limbs[:, li].copy()
+        if li + 1 < 8:
+            v |= limbs[:, li + 1] << np.uint64(32)
+        d = ((v >> np.uint64(sh)) & np.uint64((1 << b) - 1)) + carry
+        neg = d > np.uint64(1 << (b - 1))
+        mag = np.where(neg, np.uint64(1 << b) - d, d)
+        carry = neg.astype(np.uint64)
+        keys = (mag[mag > 0] - np.uint64(1)).astype(np.int64)
+        counts[w * nb:(w + 1) * nb] += np.bincount(keys, minlength=nb)
+    return counts
+
+
+def pair_round_additions(counts, rounds: int):
+    """affine additions of each batch-affine round: a bucket of m points gives floor(m / 2)
+    sums and keeps ceil(m / 2) points for the next round"""
+    m = counts.astype("int64")
+    out = []
+    for _ in range(rounds):
+        out.append(int((m // 2).sum()))
+        m = (m + 1) // 2
+    return out
 
 
 def parse():
@@ -616,29 +659,47 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
     pts = torch.cat([h, h, a])[: n1 * 16].contiguous()
     sc = scalars(n1)
     res["g1_msm_2^20_ms"] = timeit(lambda: ctx.msm_g1_dev(pts.data_ptr(), sc.data_ptr(), n1))
-    # roofline of the accumulation kernel running alone (events around each launch)
+    # roofline of the MSM's dominant kernel running alone (events around each launch): the
+    # batch-affine pair rounds when the library takes them for this size, else the XYZZ
+    # accumulation; work counted exactly from these scalars' bucket sizes
     import bendg
     L = bendg.lib()
     ctx.profile(True)
     reps = 3
     for _ in range(reps):
         ctx.msm_g1_dev(pts.data_ptr(), sc.data_ptr(), n1)
-    launches, tms = ctx.kernel_stats("msm_bucket_acc_g1")
+    stats = {f: ctx.kernel_stats(f) for f in ("msm_pair_g1", "msm_bucket_acc_g1")}
     ctx.profile(False)
     c, W = window_counts(L, n1)
-    work = n1 * W * MADD_G1_IMAD
+    rounds = L.bg_msm_pair_rounds(n1, 0)
+    counts = bucket_counts(sc.cpu().numpy().view(np.uint32).reshape(n1, 8), c)
+    pair_adds = pair_round_additions(counts, rounds)
+    if rounds:
+        kern, work = "msm_pair_g1", sum(pair_adds) * PAIR_G1_IMAD
+        model = ("%d batch-affine rounds: %s affine additions x %d IMAD (5 products + 1 square: 3 for the "
+                 "shared inversion, the slope, its square and y3), counted from the scalars' bucket sizes "
+                 "(c=%d, W=%d, %d entries)" % (rounds, "+".join(str(a) for a in pair_adds), PAIR_G1_IMAD, c, W,
+                                               int(counts.sum())))
+        where = "G1 MSM 2^20 alone: k_pair_round, %d launches per MSM timed as one span" % rounds
+    else:
+        kern, work = "msm_bucket_acc_g1", int(counts.sum()) * MADD_G1_IMAD
+        model = "%d entries x %d IMAD per mixed add (c=%d, W=%d)" % (int(counts.sum()), MADD_G1_IMAD, c, W)
+        where = "G1 MSM 2^20 alone"
+    launches, tms = stats[kern]
     avg = tms / max(1, launches)
     achieved = work / (avg * 1e-3) / 1e9
     traffic = None
     tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     if os.path.exists(tf):
-        traffic = json.load(open(tf)).get("msm_bucket_acc_g1_2^20", {}).get("bytes_per_launch")
-    res["roofline"] = {"kernel": "msm_bucket_acc_g1", "where": "G1 MSM 2^20 alone (the dominant kernel of the proof)",
+        traffic = json.load(open(tf)).get(kern + "_2^20", {}).get("bytes_per_launch")
+    res["roofline"] = {"kernel": kern, "where": where,
                        "bound": "imad", "achieved": round(achieved, 1), "peak": round(imad_peak / 1e9, 1),
                        "unit": "Gimad/s", "frac": round(achieved / (imad_peak / 1e9), 4), "traffic": traffic,
                        "work_per_launch": work, "avg_launch_ms": round(avg, 4), "launches": launches,
                        "peak_source": "bg_probe_imad on this GPU (32-bit mad.lo/mad.hi chains)",
-                       "work_model": "n W entries x %d IMAD per mixed add (c=%d, W=%d)" % (MADD_G1_IMAD, c, W),
+                       "work_model": model,
+                       "accumulation_after_rounds_ms": round(stats["msm_bucket_acc_g1"][1] /
+                                                             max(1, stats["msm_bucket_acc_g1"][0]), 4),
                        "hbm": acc_hbm_view(n1, c, W, avg, traffic)}
     if only_g1:
         return res

@@ -37,7 +37,7 @@ EXPORTS = (
     "bg_ctx_kernel_stats", "bg_probe_imad", "bg_msm_g1_noalloc", "bg_prove_batch", "bg_prove_footprint",
     "bg_server_create", "bg_server_submit", "bg_server_wait", "bg_server_reserved_bytes", "bg_server_destroy",
     "bg_ctx_timeline", "bg_msm_table_window_bits", "bg_ctx_transfer_bytes", "bg_verify", "bg_pairing",
-    "bg_msm_window_override", "bg_msm_proof_window_bits",
+    "bg_msm_window_override", "bg_msm_proof_window_bits", "bg_msm_pair_rounds_override", "bg_msm_pair_rounds",
 )
 
 
@@ -112,6 +112,8 @@ def lib():
         "bg_msm_table_window_bits": (i32, [sz, i32]),
         "bg_msm_proof_window_bits": (i32, [sz, i32]),
         "bg_msm_window_override": (i32, [vp, i32, i32, i32]),
+        "bg_msm_pair_rounds_override": (i32, [vp, i32]),
+        "bg_msm_pair_rounds": (i32, [sz, i32]),
         "bg_ctx_profile": (i32, [vp, i32]),
         "bg_ctx_timeline": (i32, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "bg_ctx_transfer_bytes": (i32, [vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
@@ -237,6 +239,11 @@ class Context:
         """force the MSM window width (layout 0: bucket set per window, 1: tables of keys uploaded
         afterwards); c = 0 restores the library's choice"""
         self._check(self._L.bg_msm_window_override(self.h, layout, curve, c), "bg_msm_window_override")
+
+    def pair_rounds_override(self, rounds: int):
+        """force the number of batch-affine pair rounds of later MSMs (-1: the library's model,
+        0: none); results do not depend on it"""
+        self._check(self._L.bg_msm_pair_rounds_override(self.h, rounds), "bg_msm_pair_rounds_override")
 
     def transfer_bytes(self):
         """(host-to-device, device-to-host) bytes copied by this context so far"""

@@ -298,11 +298,19 @@ void bg_host_free(void* p) {
 int bg_msm_window_bits(size_t n, int curve) { return msm_pick_c(n, curve == BG_CURVE_G2); }
 int bg_msm_table_window_bits(size_t n, int curve) { return msm_pick_c_table(n, curve == BG_CURVE_G2); }
 int bg_msm_proof_window_bits(size_t n, int curve) { return msm_pick_c_proof(n, curve == BG_CURVE_G2); }
+int bg_msm_pair_rounds(size_t n, int curve) { return msm_pair_rounds(n, curve == BG_CURVE_G2); }
 
 int bg_msm_window_override(bg_ctx* ctx, int layout, int curve, int c) {
   BG_ARG_CHECK(ctx, !ctx || (layout != 0 && layout != 1) || (curve != BG_CURVE_G1 && curve != BG_CURVE_G2) ||
                         (c != 0 && (c < 2 || c > 22)));
   ctx->c.c_override[layout][curve == BG_CURVE_G2 ? 1 : 0] = c;
+  return BG_OK;
+}
+
+int bg_msm_pair_rounds_override(bg_ctx* ctx, int rounds) {
+  BG_ARG_CHECK(ctx, !ctx || rounds < -1 || rounds > 12);
+  ctx->c.pair_rounds_override = rounds;
+  for (auto& lane : ctx->lanes) lane->pair_rounds_override = rounds;
   return BG_OK;
 }
 
@@ -468,6 +476,7 @@ int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnes
       std::unique_ptr<Ctx> lane(new Ctx());
       ctx_init(*lane, ctx->c.device);
       lane->shared_gpu = true;
+      lane->pair_rounds_override = ctx->c.pair_rounds_override;
       ctx->lanes.push_back(std::move(lane));
     }
     // largest domains first (longest-processing-time order) so the tail is made of small proofs

@@ -153,6 +153,9 @@ struct Ctx {
   // window widths forced for tuning (bg_msm_window_override): [0] per-window bucket sets,
   // [1] window tables of keys uploaded afterwards; [curve]; 0 = the library's choice
   int c_override[2][2] = {{0, 0}, {0, 0}};
+  // batch-affine pair rounds before each MSM's accumulation (bg_msm_pair_rounds_override):
+  // -1 = the library's cost model, 0 = none
+  int pair_rounds_override = -1;
   std::map<int, NttTables> ntt_tabs;      // per domain size, built on first use
   // optional per-kernel timing: CUDA events recorded around selected launches on their
   // own stream, resolved when the statistics are read

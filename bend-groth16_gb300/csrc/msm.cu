@@ -29,6 +29,7 @@
 #include "msm_tune.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -259,13 +260,14 @@ __global__ void __launch_bounds__(kAccThreads<F>) k_bucket_acc(const uint32_t* _
   // The next entry's point is gathered before this entry's addition, so the gather's latency
   // hides behind the arithmetic (G1 accumulation 2^20 3.88 -> 3.82 ms; 126 registers, still
   // four CTAs per SM).
-  uint32_t code = sorted[beg];
+  // sorted == nullptr: the entries are the points themselves (the output of the pair rounds)
+  uint32_t code = sorted ? sorted[beg] : beg;
   Affine<F> p = load_affine<F>(points + (size_t)(code & 0x7fffffffu) * 2 * FW);
   for (uint32_t e = beg; e < end; e++) {
     uint32_t code_n = 0;
     Affine<F> pn;
     if (e + 1 < end) {
-      code_n = sorted[e + 1];
+      code_n = sorted ? sorted[e + 1] : e + 1;
       pn = load_affine<F>(points + (size_t)(code_n & 0x7fffffffu) * 2 * FW);
     }
     if (code >> 31) p = affine_neg(p);
@@ -328,6 +330,8 @@ __global__ void __launch_bounds__(128) k_bucket_heavy(const uint32_t* __restrict
 constexpr uint32_t kHeavyThreads = 128;
 constexpr uint32_t kHeavyGrid = 152;
 
+#include "msm_pairs.cuh"
+
 // acc += value of bucket `key` (entries [offsets[key], offsets[key+1])): nothing when empty, the
 // stored bucket when it lies in one slice or is heavy, else its pieces.
 template <class F>
@@ -363,6 +367,22 @@ inline uint32_t slice_entries(size_t max_entries, size_t nkeys, double piece_us 
     }
   }
   return best;
+}
+
+// Resident threads of a pair round on the whole GPU (SMs x CTAs per SM x CTA size).
+template <class F>
+double pair_slots() {
+  static std::atomic<double> slots{0.0};
+  double s = slots.load();
+  if (s == 0.0) {
+    int dev = 0, sms = 0, occ = 0;
+    BG_CUDA(cudaGetDevice(&dev));
+    BG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    BG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pair_round<F, true>, kPairThreads<F>, 0));
+    s = (double)sms * (occ > 0 ? occ : 1) * kPairThreads<F>;
+    slots.store(s);
+  }
+  return s;
 }
 
 // Scratch of the bucket phase for at most max_entries entries (words): pieces and the heavy list.
@@ -768,15 +788,54 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   if (table) d_points = table->d;
   plan.c = so.c;
   plan.W = so.sets;
-  plan.entries = so.max_entries;
   Workspace& ws = ctx.ws;
-  uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", so.nkeys * PW);
-  const BucketScratch bs = bucket_scratch<F>(so.max_entries, so.nkeys, [&](const char* name, size_t words) {
-    return ws.get_t<uint32_t>(tag + ".slice_" + name, words);
-  });
   if (so.done) BG_CUDA(cudaStreamWaitEvent(st, so.done, 0));
   Ctx* prof = (ctx.profile || ctx.timeline) ? &ctx : nullptr;
-  bucket_accumulate<F>(prof, st, d_points, so.offsets, so.sorted, (uint32_t)so.nkeys, so.max_entries, buckets, bs);
+
+  // Batch-affine pair rounds, where the cost model (or the tuning override) takes them, halve
+  // every bucket in affine coordinates first (msm_pairs.cuh); the XYZZ accumulation, the heavy
+  // pass and the reduction then read the last level's points directly, with its offsets.
+  const uint32_t* acc_points = d_points;
+  const uint32_t* acc_sorted = so.sorted;
+  const uint32_t* acc_offsets = so.offsets;
+  size_t acc_entries = so.max_entries;
+  const int rounds = ctx.pair_rounds_override >= 0 ? ctx.pair_rounds_override
+                                                   : pair_rounds_model(so.max_entries, so.nkeys, FW == 16);
+  if (rounds > 0) {
+    constexpr int NT = kPairThreads<F>;
+    const double pslots = pair_slots<F>();
+    const uint32_t me = (uint32_t)so.max_entries;
+    const uint32_t nk = (uint32_t)so.nkeys;
+    uint32_t* lvl[2] = {ws.get_t<uint32_t>(tag + ".pairs0", level_start(me, nk, 1) * 2 * FW), nullptr};
+    if (rounds > 1) lvl[1] = ws.get_t<uint32_t>(tag + ".pairs1", level_start(me, nk, 2) * 2 * FW);
+    uint32_t* fin = ws.get_t<uint32_t>(tag + ".pair_offsets", so.nkeys + 1);
+    KernelTimer kt(ctx, FW == 8 ? "msm_pair_g1" : "msm_pair_g2", st);
+    for (int r = 0; r < rounds; r++) {
+      // Up to 256 positions per thread, in a whole number of waves of resident threads: one
+      // wave of long batches amortises each CTA's product tree and inversion best (G1 MSM 2^20
+      // round 0: 1.99 ms with 32 positions per thread in 4 waves, 1.78 ms in one wave of 118).
+      const double outs = (double)level_start(me, nk, r + 1);
+      const double waves = std::max(1.0, std::ceil(outs / (pslots * 256.0)));
+      const uint32_t per = (uint32_t)std::max(1.0, std::ceil(outs / (waves * pslots)));
+      const unsigned grid = ceil_div(ceil_div((size_t)outs, per), NT);
+      if (r == 0)
+        k_pair_round<F, true><<<grid, NT, 0, st>>>(d_points, so.sorted, so.offsets, nk, 0, per, lvl[0], rounds, fin);
+      else
+        k_pair_round<F, false><<<grid, NT, 0, st>>>(lvl[(r - 1) & 1], nullptr, so.offsets, nk, r, per, lvl[r & 1],
+                                                    rounds, nullptr);
+      BG_CHECK_LAUNCH();
+    }
+    acc_points = lvl[(rounds - 1) & 1];
+    acc_sorted = nullptr;
+    acc_offsets = fin;
+    acc_entries = level_start(me, nk, rounds);
+  }
+  plan.entries = acc_entries;
+  uint32_t* buckets = ws.get_t<uint32_t>(tag + ".buckets", so.nkeys * PW);
+  const BucketScratch bs = bucket_scratch<F>(acc_entries, so.nkeys, [&](const char* name, size_t words) {
+    return ws.get_t<uint32_t>(tag + ".slice_" + name, words);
+  });
+  bucket_accumulate<F>(prof, st, acc_points, acc_offsets, acc_sorted, (uint32_t)so.nkeys, acc_entries, buckets, bs);
 
   cudaStream_t rs = st;
   if (st_reduce && st_reduce != st) {
@@ -787,22 +846,22 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
     BG_CUDA(cudaStreamWaitEvent(st_reduce, ev, 0));
     rs = st_reduce;
   }
-  bucket_heavy<F>(prof, rs, so.offsets, buckets, bs);
+  bucket_heavy<F>(prof, rs, acc_offsets, buckets, bs);
 
   // A reduction hidden under a later accumulation keeps its CTAs at 128 threads: a 256-thread
   // CTA of ~210 registers leaves no room for an accumulation CTA on its SM for its whole
   // (latency-bound) life (K = 18 proof: caps 64 / 128 / 256 measured 11.0 / 10.8 / 10.8 ms).
   const ReduceShape rsh =
-      reduce_shape<F>(so.nb, so.sets, so.max_entries, bs.K, ctx.sm_count, plan.latency_critical ? 256u : 128u);
+      reduce_shape<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, plan.latency_critical ? 256u : 128u);
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
   uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)so.sets * J * 2 * PW);
   {
     KernelTimer kt(ctx, FW == 8 ? "msm_reduce_g1" : "msm_reduce_g2", rs);
     if constexpr (kReduceInSmem<F>)
-      k_window_reduce_sm<F><<<so.sets * J, RT, reduce_sm_bytes<F>(RT), rs>>>(so.offsets, buckets, bs.parts, bs.K,
+      k_window_reduce_sm<F><<<so.sets * J, RT, reduce_sm_bytes<F>(RT), rs>>>(acc_offsets, buckets, bs.parts, bs.K,
                                                                              so.nb, M, J, parts);
     else
-      k_window_reduce<F><<<so.sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(so.offsets, buckets, bs.parts, bs.K,
+      k_window_reduce<F><<<so.sets * J, RT, RT * PW * sizeof(uint32_t), rs>>>(acc_offsets, buckets, bs.parts, bs.K,
                                                                                so.nb, M, J, parts);
     BG_CHECK_LAUNCH();
   }
@@ -822,6 +881,17 @@ void msm_launch(Ctx& ctx, cudaStream_t st, const std::string& tag, const uint32_
   msm_sort(ctx, st, tag, d_scalars, n, c, table != nullptr, so);
   so.done = nullptr;  // same stream: already ordered
   msm_accumulate<F>(ctx, st, tag, d_points, so, plan, st_reduce, table);
+}
+
+int msm_pair_rounds_entries(size_t max_entries, size_t nkeys, bool g2) {
+  return pair_rounds_model(max_entries, nkeys, g2);
+}
+
+int msm_pair_rounds(size_t n, bool g2) {
+  if (n == 0) return 0;
+  const int c = msm_pick_c(n, g2);
+  const size_t W = 254 / c + 1;
+  return pair_rounds_model(n * W, W << (c - 1), g2);
 }
 
 int msm_pick_c_proof(size_t n, bool g2) {

@@ -51,6 +51,10 @@ int msm_pick_c(size_t n, bool g2 = false);
 int msm_pick_c_table(size_t n, bool g2 = false);
 // window width of a bucket-set-per-window MSM inside a proof (one-shot proofs)
 int msm_pick_c_proof(size_t n, bool g2 = false);
+// batch-affine pair rounds the cost model takes for a standalone MSM of n points
+int msm_pair_rounds(size_t n, bool g2 = false);
+// the same for an MSM of at most max_entries bucket entries over nkeys buckets
+int msm_pair_rounds_entries(size_t max_entries, size_t nkeys, bool g2);
 void msm_init_kernels();
 // allocate t.d (cudaMalloc) and fill it from n packed affine points on `st`; c = 0 picks the
 // window width from n

@@ -607,8 +607,13 @@ static size_t msm_footprint_c(size_t n, bool g2, int c) {
   const size_t J = nb < 32 ? 1 : nb / 32;  // most parts a reduction shape can have (RT >= 32)
   // counters, offsets, cursors, entry list, buckets, slice pieces + heavy list, window parts,
   // scan sums
+  // batch-affine pair rounds where the model takes them: levels 1 and 2 (affine points, half
+  // an XYZZ point each) and their offsets
+  const size_t pairs = msm_pair_rounds_entries(entries, nkeys, g2) == 0
+                           ? 0
+                           : (entries / 2 + nkeys) * PW / 2 + (entries / 4 + 2 * nkeys) * PW / 2 + nkeys + 1;
   const size_t words = 3 * (nkeys + 1) + entries + nkeys * PW + 2 * threads * PW + threads / 8 + 2 +
-                       W * J * 2 * PW + 2 * ((nkeys + 1) / 2048 + 1);
+                       W * J * 2 * PW + 2 * ((nkeys + 1) / 2048 + 1) + pairs;
   return words * 4;
 }
 static size_t msm_footprint(size_t n, bool g2) {

@@ -233,6 +233,15 @@ int bg_msm_proof_window_bits(size_t n, int curve);
  * per window (bg_msm_* and the MSMs of proofs without window tables), 1 = window tables of keys
  * uploaded afterwards; c = 0 restores the library's choice, else 2..22. */
 int bg_msm_window_override(bg_ctx* ctx, int layout, int curve, int c);
+/* Batch-affine pair rounds the library's cost model takes for a standalone MSM of n points of
+ * `curve` (bg_msm_g1/g2 and their _dev forms): 2 for G1 MSMs of at least 2^23 entries with at
+ * least 32 per bucket, else 0 (measured slower there on GB300). */
+int bg_msm_pair_rounds(size_t n, int curve);
+/* Tuning hook: the number of batch-affine pair rounds before each later MSM's bucket
+ * accumulation on this context and its batch lanes (each round adds the points of every bucket
+ * in pairs, in affine coordinates, sharing one field inversion per CTA); -1 restores the
+ * library's cost model, 0 turns the rounds off, at most 12.  Results do not depend on it. */
+int bg_msm_pair_rounds_override(bg_ctx* ctx, int rounds);
 
 /* ---- measurement (no counterpart in the reference, which prints only T lines) ------- */
 /* Enable (1) / disable (0) CUDA-event timing of the library's main kernels on the streams

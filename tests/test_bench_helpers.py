@@ -55,3 +55,38 @@ def test_accumulation_hbm_view():
     assert abs(r["achieved"] - r["algorithmic_bytes"] / 3.82e-3 / 1e9) < 0.1
     if r["peak"]:
         assert 0 < r["frac"] < 0.05
+
+
+def test_bucket_counts_match_the_device_digits(tmp_path):
+    """bench.bucket_counts (the exact work count of the roofline) gives each scalar the buckets
+    the device's signed-digit recoding gives it (msm.cu's digits section, compiled for the host)"""
+    import device_emul
+    lib = ctypes.CDLL(device_emul.build_digits(str(tmp_path)))
+    rng = np.random.default_rng(5)
+    n = 300
+    sc = rng.integers(0, 1 << 32, size=(n, 8), dtype=np.uint64).astype(np.uint32)
+    sc[:, 7] &= 0x0FFFFFFF
+    sc[:3] = 0
+    sc[1, 0] = 1
+    sc[2] = np.array([(o.P_FR - 1) >> (32 * i) & 0xFFFFFFFF for i in range(8)], dtype=np.uint32)
+    for c in (3, 9, 15, 17):
+        W = 254 // c + 1
+        nb = 1 << (c - 1)
+        want = np.zeros(W * nb, dtype=np.int64)
+        mags = (ctypes.c_uint32 * W)()
+        negs = (ctypes.c_uint8 * W)()
+        for i in range(n):
+            s = (ctypes.c_uint32 * 8)(*[int(v) for v in sc[i]])
+            assert lib.digits(s, W, mags, negs) == 0
+            for w in range(W):
+                if mags[w]:
+                    want[w * nb + mags[w] - 1] += 1
+        assert np.array_equal(bench.bucket_counts(sc, c), want), c
+
+
+def test_pair_round_additions():
+    counts = np.array([0, 1, 2, 3, 7, 64])
+    # round 0: 0+0+1+1+3+32 = 37 sums, leaving 0,1,1,2,4,32; round 1: 0+0+0+1+2+16 = 19
+    assert bench.pair_round_additions(counts, 2) == [37, 19]
+    assert bench.pair_round_additions(counts, 0) == []
+

@@ -64,3 +64,17 @@ def test_committed_tables_round_trip(tmp_path):
     p = tmp_path / "t.h"
     p.write_text(tune_msm.header_text(sets, tables, "test gpu", proof))
     assert tune_msm.committed_tables(str(p)) == (sets, tables, proof)
+
+
+def test_pair_round_model(built_lib):
+    """the batch-affine rounds are taken only where they measured faster on GB300: G1 MSMs of at
+    least 2^23 entries with 32 or more per bucket (bg_msm_pair_rounds is host logic, no GPU)"""
+    import bendg
+    L = bendg.lib()
+    G1, G2 = bendg.CURVE_G1, bendg.CURVE_G2
+    assert L.bg_msm_pair_rounds(1 << 20, G1) == 2     # c = 15, W = 17: 17.8 M entries, 64 per bucket
+    assert L.bg_msm_pair_rounds(1 << 22, G1) == 2
+    assert L.bg_msm_pair_rounds(1 << 18, G1) == 0     # 4.5 M entries
+    assert L.bg_msm_pair_rounds(1 << 20, G2) == 0
+    assert L.bg_msm_pair_rounds(1 << 18, G2) == 0
+    assert L.bg_msm_pair_rounds(0, G1) == 0
