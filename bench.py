@@ -106,8 +106,13 @@ def parse():
     ap.add_argument("--no-primitives", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-proof mixed-K batch measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the Poisson-arrival serving measurement")
+    ap.add_argument("--no-drop-in", action="store_true", help="skip the prove_bin / bg_prove_dir load measurement")
     ap.add_argument("--msm-only", action="store_true",
                     help="time only the standalone G1 MSM 2^20 (a small, single-kernel-family profiling target)")
+    ap.add_argument("--msm-log2n", type=int, default=20, choices=range(10, 21), metavar="10..20",
+                    help="with --msm-only: the G1 MSM's size (profiling captures of a smaller case)")
+    ap.add_argument("--pair-rounds", type=int, default=-1, choices=range(-1, 13), metavar="-1..12",
+                    help="with --msm-only: force the batch-affine pair rounds (-1: the library's model)")
     ap.add_argument("--ntt-only", action="store_true",
                     help="time only the forward NTT of 2^20 Fr elements (a single-kernel profiling target)")
     ap.add_argument("--data-root", default=os.environ.get("BG_BENCH_DATA", "/tmp/bg_bench"))
@@ -251,10 +256,12 @@ def run_ours(args, dist: Dist):
         flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
         ext = torch.cuda.ExternalStream(ctx.stream)
         ops, ms = ctx.probe_imad(0, 4096)
+        ctx.pair_rounds_override(args.pair_rounds)
         prims = primitives(ctx, files, nh, nb, args, ext, flush, ops / (ms * 1e-3), only_g1=True)
         ctx.close()
-        return {"metric": "G1 MSM 2^20 ms", "value": prims["g1_msm_2^20_ms"], "unit": "ms",
-                "higher_is_better": False, "roofline": prims["roofline"]}
+        key = "g1_msm_2^%d_ms" % args.msm_log2n
+        return {"metric": "G1 MSM 2^%d ms" % args.msm_log2n, "value": prims[key], "unit": "ms",
+                "higher_is_better": False, "pair_rounds": prims["pair_rounds"], "roofline": prims["roofline"]}
 
     # resident proving key + device witness (inputs in HBM before the timed region)
     key = ctx.pk_upload(files)
@@ -328,11 +335,11 @@ def run_ours(args, dist: Dist):
         per_launch_work = work[dom] * args.steps / max(1, nl_)
         avg_ms = tms / max(1, nl_)
         achieved = per_launch_work / (avg_ms * 1e-3) / 1e9
-        traffic = None
-        tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
-        if os.path.exists(tf):
-            traffic = json.load(open(tf)).get(dom, {}).get("bytes_per_launch")
-        roof = {"kernel": dom, "where": "inside the proof (a profiled pass of the timed proofs; shares the GPU with 4 concurrent streams)",
+        traffic, traffic_src = traffic_record(dom)
+        roof = {"kernel": dom, "traffic_source": traffic_src,
+                "where": "inside the proof (a profiled pass of the timed proofs): avg_launch_ms is the event span "
+                         "around each launch on its stream while 4 other streams run concurrently, so it is an "
+                         "upper bound of the kernel's own duration and frac a lower bound",
                 "bound": "imad", "achieved": round(achieved, 1), "peak": round(imad_peak / 1e9, 1),
                 "unit": "Gimad/s", "frac": round(achieved / (imad_peak / 1e9), 4), "traffic": traffic,
                 "work_per_launch": per_launch_work, "avg_launch_ms": round(avg_ms, 4),
@@ -365,11 +372,42 @@ def run_ours(args, dist: Dist):
            "h2d_bytes_per_step": (xfer1[0] - xfer0[0]) // args.steps,
            "d2h_bytes_per_step": (xfer1[1] - xfer0[1]) // args.steps,
            "api": "bg_prove_host (every .bin file uploaded per proof)"}
+    # Split of e2e - value: the same one-shot call with the five query sets (pk_a .. pk_l, all
+    # but 8 MB of the files) already in device memory, which bg_prove_host then copies device to
+    # device, isolates the host-to-device transfer from the one-shot MSM layout (a bucket set per
+    # window, no window tables) that the resident key's tables avoid
+    dev_sets = {nm: torch.from_numpy(files.bufs[nm].view(np.int32)).cuda()
+                for nm in ("pk_a", "pk_b1", "pk_b2", "pk_h", "pk_l")}
+    import bendg as _b
+    dev_in = _b.Inputs.from_buffer_copy(files.inputs)
+    for nm, t in dev_sets.items():
+        setattr(dev_in, nm, t.data_ptr())
+    torch.cuda.synchronize()
+    for _ in range(2):
+        ctx.prove_inputs(dev_in)
+    sets_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        ctx.prove_inputs(dev_in)
+        e1.record(ext)
+        e1.synchronize()
+        sets_ms.append(e0.elapsed_time(e1))
+    on_dev = statistics.median(sets_ms)
+    e2e["split"] = {"query_sets_in_device_memory_ms": round(on_dev, 3),
+                    "host_transfer_ms": round(e2e["value"] - on_dev, 3),
+                    "one_shot_layout_ms": round(on_dev - value, 3),
+                    "how": "e2e - (the same bg_prove_host call with the five query sets already on the device) "
+                           "= transfer; that call - value (resident key with window tables) = layout"}
+    del dev_sets
 
     prims = None if args.no_primitives else primitives(ctx, files, nh, nb, args, ext, flush, imad_peak)
     roof_iso = prims.pop("roofline") if prims else None
     batch = None if args.no_batch else batched(ctx, args, flush, ext)
     serve = None if args.no_serve else serving(ctx, args)
+    dropin = None if args.no_drop_in else drop_in(ctx, args)
 
     result = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -377,22 +415,18 @@ def run_ours(args, dist: Dist):
         "scaling": "weak", "vs_baseline": round(value / REF_GPU_K18_MS, 6),
         "vs_baseline_ref": "Bend 2 CUDA path, RTX 5090, K=18 T total 56083 ms (bend2/bench/prover_results.md:63)",
         "dtype": "u32 (exact BN254 Fr/Fq Montgomery arithmetic)", "data": "synthetic (seeded SquareChain instance)",
-        "config": {"workload": "SquareChain(2^%d) Groth16 proof: 4 G1 MSMs + 1 G2 MSM + 7 radix-2 NTTs of 2^%d"
-                               % (args.log2n, lg),
-                   "log2_constraints": args.log2n, "domain_log2": lg, "n_a": na, "n_b": nb, "n_h": nh, "n_l": nl,
-                   "seed": args.seed, "parallelism": "replicas" if dist.world > 1 else "single GPU",
-                   "l2": "flushed (512 MiB write) before every timed step",
-                   "msm_window_bits": {"g1": {str(n): L.bg_msm_table_window_bits(n, 0) for n in sorted(set(g1_sizes))},
-                                       "g2": {str(nb): L.bg_msm_table_window_bits(nb, 1)}},
-                   "msm_layout": "resident key: 2^(c w) window tables, one shared bucket set per MSM"},
+        "config": workload_config(args, lg, na, nb, nh, nl, dist.world),
+        "msm": {"window_bits": {"g1": {str(n): L.bg_msm_table_window_bits(n, 0) for n in sorted(set(g1_sizes))},
+                                "g2": {str(nb): L.bg_msm_table_window_bits(nb, 1)}},
+                "layout": "resident key: 2^(c w) window tables, one shared bucket set per MSM"},
         "proof_verified": bool(verified),
         "e2e": e2e, "roofline": roof_iso or roof, "roofline_in_proof": roof, "gpu_launches": int(launches), "clocks": clk,
         "phases_ms_median": {k: round(statistics.median(p[k] for p in phases), 3) for k in phases[0]},
         "kernels": kernel_ms, "fq_mul_rate_gops": round(fqmul_rate / 1e9, 2), "primitives": prims,
-        "batched": batch, "serving": serve,
+        "batched": batch, "serving": serve, "drop_in": dropin,
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(path, samples=1)
+        result["cpu_baseline"] = cpu_baseline(path, samples=3)
     key.release()
     files.free()
     ctx.close()
@@ -563,6 +597,7 @@ def serving(ctx, args, lanes=8, seconds=1.5):
     for _ in range(lanes):
         srv.wait(600000)
     results = []
+    served, all_reqs = {}, []
     tag = 0
     for rate in SERVE_RATES:
         n = max(12, int(rate * seconds))
@@ -586,6 +621,7 @@ def serving(ctx, args, lanes=8, seconds=1.5):
                     return
                 assert r[5] == bendg.BG_OK
                 lat[r[0]] = r[3]
+                served[r[0]] = bytes(r[1])
                 done_at.append(time.perf_counter())
 
         th = threading.Thread(target=collect)
@@ -598,6 +634,7 @@ def serving(ctx, args, lanes=8, seconds=1.5):
             srv.submit(keys[k], w, rs, tg)
         th.join()
         span = max(done_at) - t0
+        all_reqs.extend(reqs)
         vals = list(lat.values())
         results.append({"offered_rps": rate, "requests": n, "completed": len(vals),
                         "p50_ms": round(percentile(vals, 50), 2), "p99_ms": round(percentile(vals, 99), 2),
@@ -605,12 +642,78 @@ def serving(ctx, args, lanes=8, seconds=1.5):
                         "k_counts": {str(k): sum(1 for r in reqs if r[1] == k) for k in SERVE_KS}})
     reserved = srv.reserved_bytes()
     srv.close()
+    # After the timed windows: every served proof against the same request proved alone on the
+    # plain path (bit for bit), and the pairing check of one served proof per K under its vk.bin
+    import numpy as np
+    mismatch = {str(r["offered_rps"]): 0 for r in results}
+    rate_of = {}
+    base = 0
+    for r in results:
+        for t in range(base, base + r["requests"]):
+            rate_of[t] = str(r["offered_rps"])
+        base += r["requests"]
+    verified = {}
+    for tg, k, w, rs in all_reqs:
+        alone, _ = keys[k].prove(w, rs)
+        if bytes(alone) != served.get(tg):
+            mismatch[rate_of[tg]] += 1
+        if str(k) not in verified:
+            vkw = np.fromfile(os.path.join(paths[k], "vk.bin"), dtype="<u4").astype(np.uint32)
+            n_ic = int(vkw[224])
+            verified[str(k)] = bool(bendg.verify(vkw[0:32], vkw[32:96], vkw[96:160], vkw[160:224],
+                                                 vkw[225:225 + 32 * n_ic], w[16:16 * n_ic], alone))
+    for r in results:
+        r["bit_exact_vs_alone"] = mismatch[str(r["offered_rps"])] == 0
     for k in SERVE_KS:
         keys[k].release()
     return {"workload": "Poisson arrivals, K drawn from %s with weights %s (seed %d), %s s of arrivals per rate, "
                         "all five keys resident" % (list(SERVE_KS), list(SERVE_WEIGHTS), args.seed + 4, seconds),
             "lanes": lanes, "hbm_budget_bytes": budget, "reserved_scratch_bytes": reserved, "rates": results,
-            "single_proof_k20": k20}
+            "bit_exact_vs_alone": all(v == 0 for v in mismatch.values()) and len(served) == len(all_reqs),
+            "served_proofs_checked": len(all_reqs),
+            "exactness_check": "after the timed windows, every served proof compared word for word with the "
+                               "same (key, witness, r, s) proved alone by bg_prove_resident",
+            "verified_per_k": verified, "single_proof_k20": k20}
+
+
+def drop_in(ctx, args, ks=(18, 20), reps=3):
+    """The drop-in path of bend2/scripts/prove.sh: the prove_bin CLI (a new process per proof,
+    BENDG_DATA pointing at the instance's .bin files, warm page cache) and bg_prove_dir in a warm
+    process, with the T lines the library reports; the reference's T load for the same sizes is
+    883 ms (K=18) and 3,502 ms (K=20) (bend2/bench/prover_results.md:59, :60)"""
+    out = {}
+    binp = os.path.join(PKG, "prove_bin")
+    for k in ks:
+        a = argparse.Namespace(**vars(args))
+        a.log2n = k
+        single = Dist.__new__(Dist)
+        single.world, single.rank, single.local, single.pg = 1, 0, 0, None
+        path = ensure_instance(a, single, lambda kk, s, p: ctx.synth_square_chain(kk, s, p))
+        nbytes = sum(os.path.getsize(os.path.join(path, f)) for f in os.listdir(path) if f.endswith(".bin"))
+        env = dict(os.environ, BENDG_DATA=path)
+        cli = []
+        for rep in range(reps + 1):  # the first run warms the page cache
+            t0 = time.perf_counter()
+            r = subprocess.run([binp], env=env, capture_output=True, text=True, check=True)
+            wall = (time.perf_counter() - t0) * 1e3
+            T = {ln.split()[1]: float(ln.split()[2]) for ln in r.stdout.splitlines() if ln.startswith("T ")}
+            if rep:
+                cli.append((wall, T, "".join(ln + "\n" for ln in r.stdout.splitlines() if ln[:2] in ("A ", "B ", "C "))))
+        inproc = []
+        for _ in range(reps + 1):
+            proof, t = ctx.prove_dir(path)
+            inproc.append(t)
+        inproc = inproc[1:]
+        med = statistics.median
+        out["k%d" % k] = {
+            "bytes_read": nbytes,
+            "cli_wall_ms": round(med(c[0] for c in cli), 1),
+            "cli_T_load_ms": med(c[1]["load"] for c in cli), "cli_T_total_ms": med(c[1]["total"] for c in cli),
+            "in_process_T_load_ms": round(med(t["load"] for t in inproc), 2),
+            "in_process_T_total_ms": round(med(t["total"] for t in inproc), 2),
+            "same_proof_cli_and_in_process": all(c[2] == ctx.proof_text(proof) for c in cli),
+            "reference_T_load_ms": {18: 883, 20: 3502}.get(k)}
+    return out
 
 
 def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
@@ -653,12 +756,13 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
         return round(statistics.median(out), 3)
 
     res = {}
-    n1 = 1 << 20
+    lg1 = args.msm_log2n if only_g1 else 20
+    n1 = 1 << lg1
     h = packed("pk_h", nh * 32)
     a = packed("pk_a", 2 * 32)
     pts = torch.cat([h, h, a])[: n1 * 16].contiguous()
     sc = scalars(n1)
-    res["g1_msm_2^20_ms"] = timeit(lambda: ctx.msm_g1_dev(pts.data_ptr(), sc.data_ptr(), n1))
+    res["g1_msm_2^%d_ms" % lg1] = timeit(lambda: ctx.msm_g1_dev(pts.data_ptr(), sc.data_ptr(), n1))
     # roofline of the MSM's dominant kernel running alone (events around each launch): the
     # batch-affine pair rounds when the library takes them for this size, else the XYZZ
     # accumulation; work counted exactly from these scalars' bucket sizes
@@ -671,7 +775,8 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
     stats = {f: ctx.kernel_stats(f) for f in ("msm_pair_g1", "msm_bucket_acc_g1")}
     ctx.profile(False)
     c, W = window_counts(L, n1)
-    rounds = L.bg_msm_pair_rounds(n1, 0)
+    rounds = L.bg_msm_pair_rounds(n1, 0) if args.pair_rounds < 0 or not only_g1 else args.pair_rounds
+    res["pair_rounds"] = rounds
     counts = bucket_counts(sc.cpu().numpy().view(np.uint32).reshape(n1, 8), c)
     pair_adds = pair_round_additions(counts, rounds)
     if rounds:
@@ -680,19 +785,16 @@ def primitives(ctx, files, nh, nb, args, ext, flush, imad_peak, only_g1=False):
                  "shared inversion, the slope, its square and y3), counted from the scalars' bucket sizes "
                  "(c=%d, W=%d, %d entries)" % (rounds, "+".join(str(a) for a in pair_adds), PAIR_G1_IMAD, c, W,
                                                int(counts.sum())))
-        where = "G1 MSM 2^20 alone: k_pair_round, %d launches per MSM timed as one span" % rounds
+        where = "G1 MSM 2^%d alone: k_pair_round, %d launches per MSM timed as one span" % (lg1, rounds)
     else:
         kern, work = "msm_bucket_acc_g1", int(counts.sum()) * MADD_G1_IMAD
         model = "%d entries x %d IMAD per mixed add (c=%d, W=%d)" % (int(counts.sum()), MADD_G1_IMAD, c, W)
-        where = "G1 MSM 2^20 alone"
+        where = "G1 MSM 2^%d alone" % lg1
     launches, tms = stats[kern]
     avg = tms / max(1, launches)
     achieved = work / (avg * 1e-3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
-    if os.path.exists(tf):
-        traffic = json.load(open(tf)).get(kern + "_2^20", {}).get("bytes_per_launch")
-    res["roofline"] = {"kernel": kern, "where": where,
+    traffic, traffic_src = traffic_record("%s_2^%d" % (kern, lg1))
+    res["roofline"] = {"kernel": kern, "where": where, "traffic_source": traffic_src,
                        "bound": "imad", "achieved": round(achieved, 1), "peak": round(imad_peak / 1e9, 1),
                        "unit": "Gimad/s", "frac": round(achieved / (imad_peak / 1e9), 4), "traffic": traffic,
                        "work_per_launch": work, "avg_launch_ms": round(avg, 4), "launches": launches,
@@ -758,7 +860,31 @@ def ntt_roofline(lg, ms, imad_peak):
 
 
 # ---------------------------------------------------------------- CPU restatement
-def cpu_baseline(path: str, samples: int = 1) -> dict:
+def traffic_record(key: str):
+    """DRAM bytes per launch of a kernel from the committed ncu summary (profiles/
+    roofline_traffic.json), with the capture's date, commit and command: ncu cannot run inside
+    the timed bench, so the figure is as current as that capture"""
+    tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if not os.path.exists(tf):
+        return None, None
+    e = json.load(open(tf)).get(key)
+    if not e:
+        return None, None
+    return e.get("bytes_per_launch"), "%s (captured %s at commit %s)" % (e.get("source"), e.get("captured", "?"),
+                                                                       e.get("commit", "?"))
+
+
+def workload_config(args, lg, na, nb, nh, nl, world):
+    """the `config` both arms print: the same keys and values for the same workload"""
+    return {"workload": "SquareChain(2^%d) Groth16 proof: 4 G1 MSMs + 1 G2 MSM + 7 radix-2 NTTs of 2^%d"
+                        % (args.log2n, lg),
+            "log2_constraints": args.log2n, "domain_log2": lg, "n_a": na, "n_b": nb, "n_h": nh, "n_l": nl,
+            "seed": args.seed, "parallelism": "replicas" if world > 1 else "single device",
+            "l2": "inputs larger than L2 (proving key and witness, 308 MB at 2^18); the GPU arm also flushes L2 "
+                  "(512 MiB write) before every timed step"}
+
+
+def cpu_baseline(path: str, samples: int = 3) -> dict:
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_c
     threads = os.cpu_count() or 1
@@ -807,9 +933,7 @@ def run_reference(args, dist: Dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 1), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": round(value / REF_GPU_K18_MS, 6), "dtype": "u64 (exact BN254 arithmetic)",
         "data": "synthetic (seeded SquareChain instance)",
-        "config": {"workload": "SquareChain(2^%d) Groth16 proof: 4 G1 MSMs + 1 G2 MSM + 7 radix-2 NTTs of 2^%d"
-                               % (args.log2n, lg), "log2_constraints": args.log2n, "domain_log2": lg, "n_a": na,
-                   "n_b": nb, "n_h": nh, "n_l": nl, "seed": args.seed},
+        "config": workload_config(args, lg, na, nb, nh, nl, dist.world),
         "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "one complete proof per step (the reference's Bend 2 / arkworks CPU provers "
                                    "cannot run on this image: C restatement in oracle/)"},

@@ -331,6 +331,14 @@ class Context:
                     "bg_prove_dir")
         return proof, t.as_dict()
 
+    def prove_inputs(self, inputs: "Inputs"):
+        """bg_prove_host on an Inputs record whose pointers the caller set (host, pinned, or
+        device memory for the five query sets)"""
+        proof, t = Proof(), PhaseMs()
+        self._check(self._L.bg_prove_host(self.h, ctypes.byref(inputs), ctypes.byref(proof), ctypes.byref(t)),
+                    "bg_prove_host")
+        return proof, t.as_dict()
+
     def prove_host(self, files: "HostFiles"):
         proof, t = Proof(), PhaseMs()
         self._check(self._L.bg_prove_host(self.h, ctypes.byref(files.inputs), ctypes.byref(proof),

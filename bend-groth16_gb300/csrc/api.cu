@@ -10,7 +10,12 @@
 #include <thread>
 #include <vector>
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include "common.cuh"
+#include "host_pool.hpp"
 #include "pairing.hpp"
 #include "ec.cuh"
 #include "host_ff.hpp"
@@ -217,17 +222,47 @@ void ctx_release(Ctx& c) {
 
 namespace {
 
-bool read_file(const std::string& path, std::vector<char>& out) {
-  FILE* f = fopen(path.c_str(), "rb");
-  if (!f) return false;
-  fseek(f, 0, SEEK_END);
-  long sz = ftell(f);
-  fseek(f, 0, SEEK_SET);
-  out.resize(sz > 0 ? (size_t)sz : 0);
-  size_t got = sz > 0 ? fread(out.data(), 1, (size_t)sz, f) : 0;
-  fclose(f);
-  return got == out.size();
-}
+// The .bin files of one directory, opened and sized up front, then read in parallel.
+struct DirFiles {
+  static constexpr size_t kChunk = size_t(16) << 20;
+  std::vector<int> fd;
+  std::vector<size_t> size;
+  std::vector<std::string> path;
+  DirFiles(const char* dir, const char* const* names, int n) : fd(n, -1), size(n, 0), path(n) {
+    for (int i = 0; i < n; i++) {
+      path[i] = std::string(dir) + "/" + names[i] + ".bin";
+      fd[i] = open(path[i].c_str(), O_RDONLY);
+      struct stat st;
+      if (fd[i] < 0 || fstat(fd[i], &st) != 0 || st.st_size < 0) throw Error(BG_E_IO, "cannot read " + path[i]);
+      size[i] = (size_t)st.st_size;
+    }
+  }
+  ~DirFiles() {
+    for (int f : fd)
+      if (f >= 0) close(f);
+  }
+  // every file into its buffer: chunks of kChunk bytes on the host pool and the calling thread
+  void read_all(char* const* buf) {
+    std::vector<std::pair<int, size_t>> chunks;  // (file, offset)
+    for (size_t i = 0; i < fd.size(); i++)
+      for (size_t off = 0; off < size[i]; off += kChunk) chunks.emplace_back((int)i, off);
+    std::atomic<int> bad{-1};
+    HostPool::get().parallel_for((int)chunks.size(), [&](int c) {
+      const int i = chunks[c].first;
+      const size_t off = chunks[c].second, len = std::min(kChunk, size[i] - off);
+      size_t got = 0;
+      while (got < len) {
+        const ssize_t r = pread(fd[i], buf[i] + off + got, len - got, (off_t)(off + got));
+        if (r <= 0) {
+          bad.store(i);
+          return;
+        }
+        got += (size_t)r;
+      }
+    });
+    if (bad.load() >= 0) throw Error(BG_E_IO, "cannot read " + path[bad.load()]);
+  }
+};
 
 }  // namespace
 
@@ -564,11 +599,17 @@ int bg_prove_dir(bg_ctx* ctx, const char* dir, bg_proof* out, bg_phase_ms* times
     const auto t0 = std::chrono::steady_clock::now();
     static const char* names[13] = {"header", "witness", "r1cs_a", "r1cs_b", "r1cs_c", "pk_g1", "pk_g2",
                                     "pk_a",   "pk_b1",   "pk_b2",  "pk_h",   "pk_l",   "rs"};
-    std::vector<char> buf[13];
-    for (int i = 0; i < 13; i++) {
-      const std::string path = std::string(dir) + "/" + names[i] + ".bin";
-      if (!read_file(path, buf[i])) throw Error(BG_E_IO, "cannot read " + path);
-    }
+    // The files go straight into pinned host buffers cached by the context (no zero-filled
+    // pageable copy, no staging on the way to the device): the 13 files are cut into 16 MiB
+    // chunks read with pread on the host pool, and every upload of the proof is then an
+    // asynchronous copy from pinned memory that overlaps the proof (load_u32 of
+    // bend2/src/bin_io.bend:73-78 reads them one after another).
+    cudaSetDevice(ctx->c.device);
+    DirFiles files(dir, names, 13);
+    char* buf[13];
+    for (int i = 0; i < 13; i++)
+      buf[i] = ctx->c.host_cache.get_t<char>(std::string("dir.") + names[i], std::max<size_t>(files.size[i], 1));
+    files.read_all(buf);
     bg_inputs in;
     const void** ptrs[13] = {&in.header, &in.witness, &in.r1cs_a, &in.r1cs_b, &in.r1cs_c, &in.pk_g1, &in.pk_g2,
                              &in.pk_a,   &in.pk_b1,   &in.pk_b2,  &in.pk_h,   &in.pk_l,   &in.rs};
@@ -577,10 +618,9 @@ int bg_prove_dir(bg_ctx* ctx, const char* dir, bg_proof* out, bg_phase_ms* times
                          &in.pk_b1_bytes,  &in.pk_b2_bytes,   &in.pk_h_bytes,   &in.pk_l_bytes,
                          &in.rs_bytes};
     for (int i = 0; i < 13; i++) {
-      *ptrs[i] = buf[i].data();
-      *sizes[i] = buf[i].size();
+      *ptrs[i] = buf[i];
+      *sizes[i] = files.size[i];
     }
-    cudaSetDevice(ctx->c.device);
     const Header h = parse_header(in);
     validate_inputs(in, h, true);
     PkDev* pk = pk_stage_oneshot(ctx->c, in);

@@ -55,6 +55,61 @@ def test_served_results_equal_alone(ctx, keys):
         assert got[tag] == ctx.proof_text(alone)
 
 
+def test_served_mix_matches_c_oracle(ctx, tmp_path_factory):
+    """a bounded mix of the serving workload's smaller sizes (K in {12, 14, 16}) submitted while
+    earlier requests are proving: the request carrying an instance's own witness and r, s must
+    equal the C oracle's proof of that instance word for word, every other served proof the
+    same request proved alone, and one proof per K must pass the pairing verifier"""
+    import numpy as np
+    import oracle_c
+    from test_gpu_prove import proof_words
+    from test_verify import read_vk
+    rng = random.Random(1216)
+    inst = {}
+    for k in (12, 14, 16):
+        p = str(tmp_path_factory.mktemp("mix") / ("sq%d" % k))
+        ctx.synth_square_chain(k, 1200 + k, p)
+        f = bendg.HostFiles(p)
+        want, _ = oracle_c.prove_dir(p)
+        inst[k] = (p, f, ctx.pk_upload(f), want)
+    reqs = []
+    for tag in range(18):
+        k = (12, 14, 16)[tag % 3] if tag < 3 else rng.choice((12, 14, 16))
+        p, f, key, _ = inst[k]
+        if tag < 3:  # the instance's own witness and randomness: the C oracle's proof
+            w, rs = f.words("witness").copy(), f.words("rs").copy()
+        else:
+            w = square_chain_witness(k, rng.randrange(o.P_FR))
+            rs = rs_words(rng.randrange(o.P_FR), rng.randrange(o.P_FR))
+        reqs.append((tag, k, w, rs))
+    srv = bendg.Server(ctx, lanes=4)
+    for i, (tag, k, w, rs) in enumerate(reqs):
+        srv.submit(inst[k][2], w, rs, tag)
+        if i % 4 == 3:
+            time.sleep(0.003)
+    got = {}
+    while len(got) < len(reqs):
+        r = srv.wait(300000)
+        assert r is not None, "server stalled"
+        assert r[5] == bendg.BG_OK
+        got[r[0]] = proof_words(r[1]).copy()
+    srv.close()
+    verified = set()
+    for tag, k, w, rs in reqs:
+        p, f, key, want = inst[k]
+        if tag < 3:
+            assert np.array_equal(got[tag], want), k
+        alone, _ = key.prove(w, rs)
+        assert np.array_equal(got[tag], proof_words(alone)), (tag, k)
+        if k not in verified:
+            from test_verify import proof_from_words
+            assert bendg.verify(*read_vk(p), w[16:32], proof_from_words(got[tag]))
+            verified.add(k)
+    assert verified == {12, 14, 16}
+    for p, f, key, _ in inst.values():
+        key.release()
+
+
 def test_tight_budget_serialises(ctx, keys):
     fp = keys[12].footprint()
     assert fp > 0
