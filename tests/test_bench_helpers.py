@@ -90,3 +90,12 @@ def test_pair_round_additions():
     assert bench.pair_round_additions(counts, 2) == [37, 19]
     assert bench.pair_round_additions(counts, 0) == []
 
+
+
+def test_proof_imad_model(built_lib):
+    """the batch roofline's per-proof work at SquareChain(2^18): 42.0 G (G1 entries) + 20.2 G (G2)
+    + 8.1 G (NTTs) = 70.3 G multiply-adds with the committed window tables"""
+    import bendg
+    hdr = [1 << 18, 1, (1 << 18) + 1, 19, (1 << 18) + 2, (1 << 18) + 2, (1 << 19) - 1, 1 << 18]
+    w = bench.proof_imad(bendg.lib(), hdr)
+    assert abs(w - 70.28e9) < 0.01e9
