@@ -38,6 +38,7 @@ EXPORTS = (
     "bg_server_create", "bg_server_submit", "bg_server_wait", "bg_server_reserved_bytes", "bg_server_destroy",
     "bg_ctx_timeline", "bg_msm_table_window_bits", "bg_ctx_transfer_bytes", "bg_verify", "bg_pairing",
     "bg_msm_window_override", "bg_msm_proof_window_bits", "bg_msm_pair_rounds_override", "bg_msm_pair_rounds",
+    "bg_msm_coop_reduce_override",
 )
 
 
@@ -114,6 +115,7 @@ def lib():
         "bg_msm_window_override": (i32, [vp, i32, i32, i32]),
         "bg_msm_pair_rounds_override": (i32, [vp, i32]),
         "bg_msm_pair_rounds": (i32, [sz, i32]),
+        "bg_msm_coop_reduce_override": (i32, [vp, i32]),
         "bg_ctx_profile": (i32, [vp, i32]),
         "bg_ctx_timeline": (i32, [vp, i32, ctypes.c_char_p, ctypes.c_size_t]),
         "bg_ctx_transfer_bytes": (i32, [vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
@@ -244,6 +246,11 @@ class Context:
         """force the number of batch-affine pair rounds of later MSMs (-1: the library's model,
         0: none); results do not depend on it"""
         self._check(self._L.bg_msm_pair_rounds_override(self.h, rounds), "bg_msm_pair_rounds_override")
+
+    def coop_reduce_override(self, mode: int):
+        """latency-critical window reductions on groups of 8 lanes per addition: -1 the
+        library's model, 0 never, 1 always; results do not depend on it"""
+        self._check(self._L.bg_msm_coop_reduce_override(self.h, mode), "bg_msm_coop_reduce_override")
 
     def transfer_bytes(self):
         """(host-to-device, device-to-host) bytes copied by this context so far"""

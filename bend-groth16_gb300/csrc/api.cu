@@ -342,6 +342,13 @@ int bg_msm_window_override(bg_ctx* ctx, int layout, int curve, int c) {
   return BG_OK;
 }
 
+int bg_msm_coop_reduce_override(bg_ctx* ctx, int mode) {
+  BG_ARG_CHECK(ctx, !ctx || mode < -1 || mode > 1);
+  ctx->c.coop_reduce = mode;
+  for (auto& lane : ctx->lanes) lane->coop_reduce = mode;
+  return BG_OK;
+}
+
 int bg_msm_pair_rounds_override(bg_ctx* ctx, int rounds) {
   BG_ARG_CHECK(ctx, !ctx || rounds < -1 || rounds > 12);
   ctx->c.pair_rounds_override = rounds;
@@ -512,6 +519,7 @@ int bg_prove_batch(bg_ctx* ctx, bg_pk* const* pks, const uint32_t* const* witnes
       ctx_init(*lane, ctx->c.device);
       lane->shared_gpu = true;
       lane->pair_rounds_override = ctx->c.pair_rounds_override;
+      lane->coop_reduce = ctx->c.coop_reduce;
       ctx->lanes.push_back(std::move(lane));
     }
     // largest domains first (longest-processing-time order) so the tail is made of small proofs

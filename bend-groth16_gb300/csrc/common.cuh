@@ -156,6 +156,9 @@ struct Ctx {
   // batch-affine pair rounds before each MSM's accumulation (bg_msm_pair_rounds_override):
   // -1 = the library's cost model, 0 = none
   int pair_rounds_override = -1;
+  // cooperative window reductions for latency-critical MSMs (bg_msm_coop_reduce_override):
+  // -1 = the library's model, 0 = never, 1 = always
+  int coop_reduce = -1;
   std::map<int, NttTables> ntt_tabs;      // per domain size, built on first use
   // optional per-kernel timing: CUDA events recorded around selected launches on their
   // own stream, resolved when the statistics are read

@@ -654,6 +654,8 @@ constexpr bool kReduceInSmem = FieldWords<F>::value == 16;
 // on one GPU thread).
 struct ReduceShape {
   uint32_t RT, M, J;
+  double cost = 0;     // the model's latency, in dependent additions
+  bool coop = false;   // k_window_reduce_coop: RT groups of 8 lanes
 };
 template <class F>
 int reduce_blocks_per_sm(uint32_t RT) {
@@ -691,8 +693,49 @@ ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, uint32_t K, int 
       const double cost = waves * (M * per_bucket + 2.0 * lrt + lm) + 3.0 * J * sets / 16.0;
       if (cost < best_cost) {
         best_cost = cost;
-        best = {RT, M, J};
+        best = {RT, M, J, cost, false};
       }
+    }
+  }
+  best.cost = best_cost;
+  return best;
+}
+
+#include "msm_coop.cuh"
+
+// The cooperative form's shape by the same model: RT groups (of 8 lanes) per CTA, each addition
+// about kCoopAddCost of a thread's addition (dependency depth 4.6 of 14 products, plus the
+// group's exchanges), the log2 M doublings on one lane at full cost.
+constexpr double kCoopAddCost = 0.45;
+template <class F>
+int reduce_coop_blocks_per_sm(uint32_t RT) {
+  static int cache[6] = {};
+  int lrt = 0;
+  while ((1u << lrt) < RT) lrt++;
+  if (!cache[lrt]) {
+    int n = 0;
+    BG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_window_reduce_coop<F>, (int)RT * kCoopLanes,
+                                                          RT * coop_group_words<F>() * sizeof(uint32_t)));
+    cache[lrt] = n > 0 ? n : 1;
+  }
+  return cache[lrt];
+}
+template <class F>
+ReduceShape reduce_shape_coop(uint32_t nb, int sets, size_t entries, uint32_t K, int sm_count) {
+  const double e = (double)entries / ((double)nb * sets);
+  const double per_bucket = 2.0 + e / K;
+  ReduceShape best{0, 0, 0, 1e300, true};
+  for (uint32_t RT = 4; RT <= 32; RT <<= 1) {
+    for (uint32_t M = 1; M <= 16; M <<= 1) {
+      if ((uint64_t)RT * M > nb) continue;
+      const uint32_t J = nb / (RT * M);
+      int lrt = 0, lm = 0;
+      while ((1u << lrt) < RT) lrt++;
+      while ((1u << lm) < M) lm++;
+      const double slots = (double)sm_count * reduce_coop_blocks_per_sm<F>(RT);
+      const double waves = std::ceil((double)J * sets / slots);
+      const double cost = waves * (kCoopAddCost * (M * per_bucket + 2.0 * lrt) + lm) + 3.0 * J * sets / 16.0;
+      if (cost < best.cost) best = {RT, M, J, cost, true};
     }
   }
   return best;
@@ -851,13 +894,21 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   // A reduction hidden under a later accumulation keeps its CTAs at 128 threads: a 256-thread
   // CTA of ~210 registers leaves no room for an accumulation CTA on its SM for its whole
   // (latency-bound) life (K = 18 proof: caps 64 / 128 / 256 measured 11.0 / 10.8 / 10.8 ms).
-  const ReduceShape rsh =
+  ReduceShape rsh =
       reduce_shape<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, plan.latency_critical ? 256u : 128u);
+  // a reduction that ends a critical path may take the cooperative form (8 lanes per addition)
+  if (plan.latency_critical && ctx.coop_reduce != 0) {
+    const ReduceShape csh = reduce_shape_coop<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count);
+    if (ctx.coop_reduce > 0 || csh.cost < rsh.cost) rsh = csh;
+  }
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;
   uint32_t* parts = ws.get_t<uint32_t>(tag + ".parts", (size_t)so.sets * J * 2 * PW);
   {
     KernelTimer kt(ctx, FW == 8 ? "msm_reduce_g1" : "msm_reduce_g2", rs);
-    if constexpr (kReduceInSmem<F>)
+    if (rsh.coop)
+      k_window_reduce_coop<F><<<so.sets * J, RT * kCoopLanes, RT * coop_group_words<F>() * sizeof(uint32_t), rs>>>(
+          acc_offsets, buckets, bs.parts, bs.K, so.nb, M, J, parts);
+    else if constexpr (kReduceInSmem<F>)
       k_window_reduce_sm<F><<<so.sets * J, RT, reduce_sm_bytes<F>(RT), rs>>>(acc_offsets, buckets, bs.parts, bs.K,
                                                                              so.nb, M, J, parts);
     else

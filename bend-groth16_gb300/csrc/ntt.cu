@@ -17,6 +17,8 @@
 // so iNTT followed by a coset NTT needs no permutation: the coset factor g^j of coefficient j
 // is applied in bit-reversed position, fused with n^-1 into the last DIF pass.  Only the final
 // h needs one bit-reversal gather.
+#include <mutex>
+
 #include "common.cuh"
 #include "fp.cuh"
 #include "host_ff.hpp"
@@ -324,12 +326,18 @@ static void launch_pass(Ctx& ctx, cudaStream_t st, bool dit, uint32_t* d, const 
   BG_CHECK_LAUNCH();
 }
 
+// the opt-in to 32 KiB of dynamic shared memory holds for the device current when it is set:
+// once per device, safely from several host threads (batch lanes, server threads)
 void ntt_init_kernels() {
-  static bool done = false;
-  if (done) return;
-  BG_CUDA(cudaFuncSetAttribute(k_ntt_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNttTile * 32));
-  BG_CUDA(cudaFuncSetAttribute(k_ntt_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNttTile * 32));
-  done = true;
+  constexpr int kMaxDevices = 64;
+  static std::once_flag once[kMaxDevices];
+  int dev = 0;
+  BG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) throw Error(BG_E_ARG, "ntt: device index out of range");
+  std::call_once(once[dev], [] {
+    BG_CUDA(cudaFuncSetAttribute(k_ntt_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNttTile * 32));
+    BG_CUDA(cudaFuncSetAttribute(k_ntt_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNttTile * 32));
+  });
 }
 
 // DIF passes (natural -> bit-reversed).  `first_pre` scales on load in the first pass;

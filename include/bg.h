@@ -242,6 +242,11 @@ int bg_msm_pair_rounds(size_t n, int curve);
  * in pairs, in affine coordinates, sharing one field inversion per CTA); -1 restores the
  * library's cost model, 0 turns the rounds off, at most 12.  Results do not depend on it. */
 int bg_msm_pair_rounds_override(bg_ctx* ctx, int rounds);
+/* Tuning hook: the window reductions that end a critical path (standalone MSMs, a proof's last
+ * MSM, every MSM of a small proof) may run each point addition on a group of 8 cooperating
+ * lanes; mode -1 lets the library's latency model choose (the default), 0 never, 1 always
+ * (for those reductions).  Results do not depend on it. */
+int bg_msm_coop_reduce_override(bg_ctx* ctx, int mode);
 
 /* ---- measurement (no counterpart in the reference, which prints only T lines) ------- */
 /* Enable (1) / disable (0) CUDA-event timing of the library's main kernels on the streams
