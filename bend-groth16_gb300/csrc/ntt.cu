@@ -79,11 +79,16 @@ BG_DEV Fr tile_load(const uint32_t* sm, int E, int e) {
 
 // One pass: stages [s0, s0 + k) of a size-2^L transform.  A CTA owns G independent groups of
 // 2^k elements; group element t of group (hi, lo) sits at hi*2^(s0+k) + t*2^s0 + lo.
-template <bool DIT>
-__global__ void __launch_bounds__(kNttThreads) k_ntt_pass(uint32_t* __restrict__ data, const uint32_t* __restrict__ tw,
-                                                          int L, int s0, int k, int G, int pre_mode, int post_mode,
-                                                          ScaleTab sc) {
+// Up to three vectors transformed by one launch (the QAP's a, b and c), blockIdx.y picks one.
+struct NttVecs {
+  uint32_t* p[3];
+};
+
+template <bool DIT, int NT>
+__global__ void __launch_bounds__(NT) k_ntt_pass(NttVecs vecs, const uint32_t* __restrict__ tw, int L, int s0, int k,
+                                                 int G, int pre_mode, int post_mode, ScaleTab sc) {
   extern __shared__ __align__(16) uint32_t sm[];
+  uint32_t* __restrict__ data = vecs.p[blockIdx.y];
   const int E = G << k;
   const uint32_t kmask = (1u << k) - 1u;
   const size_t lomask = (size_t(1) << s0) - 1;
@@ -284,45 +289,60 @@ NttTables& ntt_tables(Ctx& ctx, int L) {
 
 struct PassPlan {
   int s0, k, G;
+  int nt = kNttThreads;  // threads per CTA
 };
 
+// Small domains (at most 2^kSmallMaxL elements, a small proof's QAP) are a chain of
+// latency-bound transforms: they take 128-element tiles of 64 threads, one butterfly per thread
+// per stage and at most 7 stages per pass, so a pass spreads over many SMs.  The 1024-element
+// tiles give a 2^11 transform two passes of two CTAs each, every thread doing two butterflies
+// per stage; one CTA of 1024 threads over the whole vector measured 60-70 us per transform,
+// the SM's issue rate spread over 1024 butterflies a stage.
+constexpr int kSmallMaxL = 14;
+constexpr int kSmallTile = 128;
+
 static std::vector<PassPlan> plan_passes(int L) {
+  const bool small = L <= kSmallMaxL;
+  const int tile = small ? kSmallTile : kNttTile;
+  const int kmax = small ? 7 : kContigMax;
   std::vector<PassPlan> out;
-  const int k0 = std::min(L, kContigMax);
+  auto add = [&](int s0, int k, int G) {
+    PassPlan p{s0, k, G};
+    p.nt = small ? std::max(32, (G << k) / 2) : kNttThreads;
+    out.push_back(p);
+  };
+  const int k0 = std::min(L, kmax);
   {
-    int G = kNttTile >> k0;
+    int G = tile >> k0;
     const int groups = 1 << (L - k0);
     if (G > groups) G = groups;
     if (G < 1) G = 1;
-    out.push_back({0, k0, G});
+    add(0, k0, G);
   }
   int rest = L - k0;
   int s0 = k0;
-  const int npass = (rest + kStridedMax - 1) / kStridedMax;
+  const int npass = (rest + kmax - 1) / kmax;
   for (int p = 0; p < npass; p++) {
     const int k = (rest + (npass - p) - 1) / (npass - p);
-    int G = kNttTile >> k;
+    int G = tile >> k;
     const int lo_count = 1 << s0;
     if (G > lo_count) G = lo_count;
-    out.push_back({s0, k, G});
+    add(s0, k, G);
     s0 += k;
     rest -= k;
   }
   return out;
 }
 
-static void launch_pass(Ctx& ctx, cudaStream_t st, bool dit, uint32_t* d, const uint32_t* tw, int L,
+static void launch_pass(Ctx& ctx, cudaStream_t st, bool dit, const NttVecs& v, int nvec, const uint32_t* tw, int L,
                         const PassPlan& p, int pre, int post, const ScaleTab& sc) {
   const size_t n = size_t(1) << L;
   const int E = p.G << p.k;
-  const unsigned blocks = (unsigned)(n / E);
+  const dim3 grid((unsigned)(n / E), (unsigned)nvec);
   const size_t smem = (size_t)E * 32;
   KernelTimer kt(ctx, "ntt_pass", st);
-  if (dit) {
-    k_ntt_pass<true><<<blocks, kNttThreads, smem, st>>>(d, tw, L, p.s0, p.k, p.G, pre, post, sc);
-  } else {
-    k_ntt_pass<false><<<blocks, kNttThreads, smem, st>>>(d, tw, L, p.s0, p.k, p.G, pre, post, sc);
-  }
+  if (dit) k_ntt_pass<true, kNttThreads><<<grid, p.nt, smem, st>>>(v, tw, L, p.s0, p.k, p.G, pre, post, sc);
+  else k_ntt_pass<false, kNttThreads><<<grid, p.nt, smem, st>>>(v, tw, L, p.s0, p.k, p.G, pre, post, sc);
   BG_CHECK_LAUNCH();
 }
 
@@ -335,14 +355,16 @@ void ntt_init_kernels() {
   BG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) throw Error(BG_E_ARG, "ntt: device index out of range");
   std::call_once(once[dev], [] {
-    BG_CUDA(cudaFuncSetAttribute(k_ntt_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNttTile * 32));
-    BG_CUDA(cudaFuncSetAttribute(k_ntt_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNttTile * 32));
+    BG_CUDA(cudaFuncSetAttribute(k_ntt_pass<true, kNttThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kNttTile * 32));
+    BG_CUDA(cudaFuncSetAttribute(k_ntt_pass<false, kNttThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kNttTile * 32));
   });
 }
 
 // DIF passes (natural -> bit-reversed).  `first_pre` scales on load in the first pass;
 // `last_post` scales on store in the last (contiguous) pass.
-static void dif(Ctx& ctx, cudaStream_t st, uint32_t* d, const uint32_t* tw, int L, int first_pre,
+static void dif(Ctx& ctx, cudaStream_t st, const NttVecs& v, int nvec, const uint32_t* tw, int L, int first_pre,
                 const ScaleTab& pre_sc, int last_post, const ScaleTab& post_sc) {
   auto plan = plan_passes(L);
   for (int i = (int)plan.size() - 1; i >= 0; i--) {
@@ -351,17 +373,18 @@ static void dif(Ctx& ctx, cudaStream_t st, uint32_t* d, const uint32_t* tw, int 
       // one pass: both scalings come from different tables; apply pre separately if needed
       if (first_pre != SC_NONE && last_post != SC_NONE)
         throw Error(BG_E_ARG, "ntt: pre and post scaling in a single-pass transform");
-      launch_pass(ctx, st, false, d, tw, L, plan[i], first_pre, last_post, first_pre ? pre_sc : post_sc);
+      launch_pass(ctx, st, false, v, nvec, tw, L, plan[i], first_pre, last_post, first_pre ? pre_sc : post_sc);
     } else {
-      launch_pass(ctx, st, false, d, tw, L, plan[i], first ? first_pre : SC_NONE, last ? last_post : SC_NONE,
+      launch_pass(ctx, st, false, v, nvec, tw, L, plan[i], first ? first_pre : SC_NONE, last ? last_post : SC_NONE,
                   first ? pre_sc : post_sc);
     }
   }
 }
 
-static void dit(Ctx& ctx, cudaStream_t st, uint32_t* d, const uint32_t* tw, int L) {
+static void dit(Ctx& ctx, cudaStream_t st, const NttVecs& v, int nvec, const uint32_t* tw, int L) {
   auto plan = plan_passes(L);
-  for (size_t i = 0; i < plan.size(); i++) launch_pass(ctx, st, true, d, tw, L, plan[i], SC_NONE, SC_NONE, ScaleTab{});
+  for (size_t i = 0; i < plan.size(); i++)
+    launch_pass(ctx, st, true, v, nvec, tw, L, plan[i], SC_NONE, SC_NONE, ScaleTab{});
 }
 
 void ntt_run(Ctx& ctx, cudaStream_t st, uint32_t* d_data, int L, int mode) {
@@ -371,24 +394,25 @@ void ntt_run(Ctx& ctx, cudaStream_t st, uint32_t* d_data, int L, int mode) {
   const size_t n = size_t(1) << L;
   uint32_t* tmp = ctx.ws.get_t<uint32_t>("ntt.tmp", n * 8);
   ScaleTab none;
+  const NttVecs v{{d_data, d_data, d_data}};
   switch (mode) {
     case BG_NTT_FORWARD:
-      dif(ctx, st, d_data, T.tw_fwd, L, SC_NONE, none, SC_NONE, none);
+      dif(ctx, st, v, 1, T.tw_fwd, L, SC_NONE, none, SC_NONE, none);
       break;
     case BG_NTT_INVERSE: {
       ScaleTab c;
       c.hi = T.ninv;
-      dif(ctx, st, d_data, T.tw_inv, L, SC_NONE, none, SC_CONST, c);
+      dif(ctx, st, v, 1, T.tw_inv, L, SC_NONE, none, SC_CONST, c);
       break;
     }
     case BG_NTT_COSET_FORWARD: {
       ScaleTab c{T.g_lo, T.g_hi, T.coset_bits};
-      dif(ctx, st, d_data, T.tw_fwd, L, SC_NATURAL, c, SC_NONE, none);
+      dif(ctx, st, v, 1, T.tw_fwd, L, SC_NATURAL, c, SC_NONE, none);
       break;
     }
     case BG_NTT_COSET_INVERSE: {
       ScaleTab c{T.gi_lo, T.gi_hi_ninv, T.coset_bits};
-      dif(ctx, st, d_data, T.tw_inv, L, SC_NONE, none, SC_BITREV, c);
+      dif(ctx, st, v, 1, T.tw_inv, L, SC_NONE, none, SC_BITREV, c);
       break;
     }
     default:
@@ -408,14 +432,15 @@ void qap_h_run(Ctx& ctx, cudaStream_t st, uint32_t* d_a, uint32_t* d_b, uint32_t
   ScaleTab none;
   ScaleTab to_coset{T.g_lo, T.g_hi_ninv, T.coset_bits};
   ScaleTab from_coset{T.gi_lo, T.gi_hi_ninv, T.coset_bits};
-  uint32_t* v[3] = {d_a, d_b, d_c};
-  for (int i = 0; i < 3; i++) {
-    dif(ctx, st, v[i], T.tw_inv, L, SC_NONE, none, SC_BITREV, to_coset);  // iNTT, then * n^-1 g^j
-    dit(ctx, st, v[i], T.tw_fwd, L);                                      // NTT on the coset
-  }
+  // a, b and c are transformed by the same launches (grid y = 3): each pass fills three times
+  // the CTAs, and a small proof's QAP is 8 launches instead of 16
+  const NttVecs abc{{d_a, d_b, d_c}};
+  dif(ctx, st, abc, 3, T.tw_inv, L, SC_NONE, none, SC_BITREV, to_coset);  // iNTT, then * n^-1 g^j
+  dit(ctx, st, abc, 3, T.tw_fwd, L);                                      // NTT on the coset
   k_qap_pointwise<<<ceil_div(n, 256), 256, 0, st>>>(d_a, d_b, d_c, T.zinv, n);
   BG_CHECK_LAUNCH();
-  dif(ctx, st, d_a, T.tw_inv, L, SC_NONE, none, SC_BITREV, from_coset);  // coset iNTT
+  const NttVecs a{{d_a, d_a, d_a}};
+  dif(ctx, st, a, 1, T.tw_inv, L, SC_NONE, none, SC_BITREV, from_coset);  // coset iNTT
   k_bitrev<<<ceil_div(n, 256), 256, 0, st>>>(d_a, d_h, L, n);
   BG_CHECK_LAUNCH();
 }

@@ -25,6 +25,7 @@
 #include "common.cuh"
 #include "ec.cuh"
 #include "host_ff.hpp"
+#include "host_pool.hpp"
 #include "msm.h"
 #include "ntt.h"
 #include "prims.h"
@@ -534,12 +535,20 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     const Fe prod = bgh::fe_from_mont(bgh::FR, bgh::fe_mul(bgh::FR, rm, sm));
     for (int i = 0; i < 4; i++) rs[i] = prod.v[i];
   }
+  // The four products of the key's delta points by r, s and r s are independent double-and-add
+  // chains of about 380 host point operations each (the G2 one three times as long): they run
+  // at once on the host pool.  A small proof's device work is shorter than them one after
+  // another (SquareChain(2^10): kernels end about 0.72 ms into the proof).
   const Xyzz<FqOps> dj = bgh::xyzz_from(pk.delta);
   const Xyzz<Fq2Ops> dj2 = bgh::xyzz_from(pk.delta2);
-  const Xyzz<FqOps> r_delta = bgh::xyzz_mul(dj, r);
-  const Xyzz<FqOps> s_delta = bgh::xyzz_mul(dj, s);
-  const Xyzz<FqOps> rs_delta = bgh::xyzz_mul(dj, rs);
-  const Xyzz<Fq2Ops> s_delta2 = bgh::xyzz_mul(dj2, s);
+  Xyzz<FqOps> r_delta, s_delta, rs_delta;
+  Xyzz<Fq2Ops> s_delta2;
+  HostPool::get().parallel_for(4, [&](int i) {
+    if (i == 0) s_delta2 = bgh::xyzz_mul(dj2, s);
+    else if (i == 1) r_delta = bgh::xyzz_mul(dj, r);
+    else if (i == 2) s_delta = bgh::xyzz_mul(dj, s);
+    else rs_delta = bgh::xyzz_mul(dj, rs);
+  });
 
   // ---- finish each MSM on the host as soon as its reduction stream drains (accumulation order
   // a, b1, b2, l, h); everything that does not need msm_h -- A, B1, B2 and s A + r B1 - r s delta
@@ -559,7 +568,12 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
   drain(plan[1]);
   msm_finish<Fq>(plan[1], res[1]);
   const Xyzz<FqOps> B1 = bgh::xyzz_add(bgh::xyzz_add(g1(res[1]), s_delta), bgh::xyzz_from(pk.beta));
-  Xyzz<FqOps> c_part = bgh::xyzz_add(bgh::xyzz_add(bgh::xyzz_mul(A, s), bgh::xyzz_mul(B1, r)), bgh::xyzz_neg(rs_delta));
+  Xyzz<FqOps> sA, rB1;
+  HostPool::get().parallel_for(2, [&](int i) {
+    if (i == 0) sA = bgh::xyzz_mul(A, s);
+    else rB1 = bgh::xyzz_mul(B1, r);
+  });
+  Xyzz<FqOps> c_part = bgh::xyzz_add(bgh::xyzz_add(sA, rB1), bgh::xyzz_neg(rs_delta));
   drain(plan[2]);
   msm_finish<Fq2>(plan[2], res[2]);
   const Xyzz<Fq2Ops> B2 = bgh::xyzz_add(
