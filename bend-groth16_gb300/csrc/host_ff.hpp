@@ -275,6 +275,21 @@ Xyzz<F> xyzz_mul(const Xyzz<F>& p, const uint64_t k[4]) {
   return r;
 }
 
+// k*P for a 64-bit k, the same 4-bit fixed window
+template <class F>
+Xyzz<F> xyzz_mul64(const Xyzz<F>& p, uint64_t k) {
+  Xyzz<F> tab[16];
+  tab[0] = xyzz_inf<F>();
+  for (int i = 1; i < 16; i++) tab[i] = xyzz_add(tab[i - 1], p);
+  Xyzz<F> r = xyzz_inf<F>();
+  for (int i = 15; i >= 0; i--) {
+    for (int d = 0; d < 4; d++) r = xyzz_dbl(r);
+    const unsigned nib = (unsigned)(k >> (4 * i)) & 15u;
+    if (nib) r = xyzz_add(r, tab[nib]);
+  }
+  return r;
+}
+
 // ---------------------------------------------------------------- wire-format conversion
 // FORMAT.md element: 16 words, each a 16-bit limb (bend2/FORMAT.md:7-8)
 inline Fe fe_from_words16(const uint32_t* w) {

@@ -25,6 +25,11 @@ struct PkDev {
   CsrDev ca, cb, cc;
   bgh::Aff<bgh::FqOps> alpha, beta, delta;
   bgh::Aff<bgh::Fq2Ops> beta2, delta2;
+  // resident keys: 2^(64 j) delta and 2^(64 j) delta2 (j < 4), so that each host product of a
+  // delta point by r, s or r s splits into four independent 64-bit pieces
+  bool delta_pow_ready = false;
+  bgh::Xyzz<bgh::FqOps> delta_pow[4];
+  bgh::Xyzz<bgh::Fq2Ops> delta2_pow[4];
   // window tables of the five query sets (a, b1, b2, h, l), built for resident keys
   MsmTable tab[5];
   bool tables = false;
