@@ -896,8 +896,17 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   // (latency-bound) life (K = 18 proof: caps 64 / 128 / 256 measured 11.0 / 10.8 / 10.8 ms).
   ReduceShape rsh =
       reduce_shape<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, plan.latency_critical ? 256u : 128u);
+  // A reduction meant to run under later accumulations that the latency model says outlasts
+  // them (a mid-size proof's G2 MSM: SquareChain(2^14)'s took 1.02 ms after 0.39 ms of
+  // remaining accumulations) is critical after all.  Latency of one dependent addition at a
+  // reduction's occupancy: about 11 us (G1), 29 us (G2), measured on GB300.
+  bool critical = plan.latency_critical;
+  if (!critical && plan.hidden_us > 0 && rsh.cost * (FW == 16 ? 29.0 : 11.0) > plan.hidden_us) {
+    critical = true;
+    rsh = reduce_shape<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, 256u);
+  }
   // a reduction that ends a critical path may take the cooperative form (8 lanes per addition)
-  if (plan.latency_critical && ctx.coop_reduce != 0) {
+  if (critical && ctx.coop_reduce != 0) {
     const ReduceShape csh = reduce_shape_coop<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count);
     if (ctx.coop_reduce > 0 || csh.cost < rsh.cost) rsh = csh;
   }

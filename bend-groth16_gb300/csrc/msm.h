@@ -22,6 +22,10 @@ struct MsmPlan {
   // small CTAs; true: it is the tail of the caller's critical path and takes the shape with
   // the shortest dependent chain
   bool latency_critical = true;
+  // for a reduction that is not latency-critical: the accumulation work (us) queued after it
+  // on the accumulation stream, which it should finish under; a longer reduction by the latency
+  // model is treated as critical (0 = no budget known: trust latency_critical)
+  double hidden_us = 0;
 };
 
 // Window table of a fixed point set: row w (w < W) holds 2^(o_w) P_i for all i (o_w the bit

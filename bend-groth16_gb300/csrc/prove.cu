@@ -495,8 +495,15 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     cudaStream_t red = ctx.side[1 + j];
     cudaStream_t ast = overlap ? red : acc_st;
     MsmPlan& p = plan[jb.idx];
-    // only msm_h's reduction is not hidden under a later accumulation; overlapped, none is
+    // only msm_h's reduction is not hidden under a later accumulation; overlapped, none is.  The
+    // others get the accumulation time queued after them (entries x about 0.3 ns for G1 and
+    // 0.9 ns for G2 inside a proof), which the reduction should not outlast.
     p.latency_critical = overlap || j == 4;
+    // (Batch and server lanes keep the fixed rule: other proofs fill the GPU there.)
+    p.hidden_us = 0;
+    if (!ctx.shared_gpu)
+      for (int k = j + 1; k < 5; k++)
+        p.hidden_us += (double)jobs[k].n * (254 / width(jobs[k]) + 1) * (jobs[k].g2 ? 0.9e-3 : 0.3e-3);
     if (overlap) BG_CUDA(cudaStreamWaitEvent(ast, ev_scalars, 0));
     if (pk.ready[jb.idx]) BG_CUDA(cudaStreamWaitEvent(ast, pk.ready[jb.idx], 0));
     t_msm[jb.idx].start(ast);
