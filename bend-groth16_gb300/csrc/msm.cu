@@ -674,8 +674,21 @@ int reduce_blocks_per_sm(uint32_t RT) {
   }
   return cache[lrt];
 }
+// The host's part of a reduction, in device additions: J parts per bucket set, 3 host additions
+// each at about 1/16 of a device addition's latency.  With `pooled`, a single bucket set of a
+// power-of-two J >= 32 (window tables) counts as msm_finish sums it: in chunks on the host pool,
+// so its latency is a chunk's parts plus the chunks' join.
+inline double host_parts_cost(uint32_t J, int sets, bool pooled) {
+  if (pooled && sets == 1 && J >= 32 && (J & (J - 1)) == 0) {
+    const uint32_t chunks = std::min<uint32_t>(16, J / 8), C = J / chunks;
+    return 3.0 * (C + chunks) / 16.0;
+  }
+  return 3.0 * J * sets / 16.0;
+}
+
 template <class F>
-ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, uint32_t K, int sm_count, uint32_t max_rt) {
+ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, uint32_t K, int sm_count, uint32_t max_rt,
+                         bool pooled_host = false) {
   const double e = (double)entries / ((double)nb * sets);
   const double per_bucket = 2.0 + e / K;
   ReduceShape best{nb < 32 ? nb : 32, 1, 1};
@@ -690,7 +703,7 @@ ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, uint32_t K, int 
       while ((1u << lm) < M) lm++;
       const double slots = (double)sm_count * reduce_blocks_per_sm<F>(RT);
       const double waves = std::ceil((double)J * sets / slots);
-      const double cost = waves * (M * per_bucket + 2.0 * lrt + lm) + 3.0 * J * sets / 16.0;
+      const double cost = waves * (M * per_bucket + 2.0 * lrt + lm) + host_parts_cost(J, sets, pooled_host);
       if (cost < best_cost) {
         best_cost = cost;
         best = {RT, M, J, cost, false};
@@ -721,7 +734,7 @@ int reduce_coop_blocks_per_sm(uint32_t RT) {
   return cache[lrt];
 }
 template <class F>
-ReduceShape reduce_shape_coop(uint32_t nb, int sets, size_t entries, uint32_t K, int sm_count) {
+ReduceShape reduce_shape_coop(uint32_t nb, int sets, size_t entries, uint32_t K, int sm_count, bool pooled_host) {
   const double e = (double)entries / ((double)nb * sets);
   const double per_bucket = 2.0 + e / K;
   ReduceShape best{0, 0, 0, 1e300, true};
@@ -734,7 +747,8 @@ ReduceShape reduce_shape_coop(uint32_t nb, int sets, size_t entries, uint32_t K,
       while ((1u << lm) < M) lm++;
       const double slots = (double)sm_count * reduce_coop_blocks_per_sm<F>(RT);
       const double waves = std::ceil((double)J * sets / slots);
-      const double cost = waves * (kCoopAddCost * (M * per_bucket + 2.0 * lrt) + lm) + 3.0 * J * sets / 16.0;
+      const double cost =
+          waves * (kCoopAddCost * (M * per_bucket + 2.0 * lrt) + lm) + host_parts_cost(J, sets, pooled_host);
       if (cost < best.cost) best = {RT, M, J, cost, true};
     }
   }
@@ -900,14 +914,21 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   // them (a mid-size proof's G2 MSM: SquareChain(2^14)'s took 1.02 ms after 0.39 ms of
   // remaining accumulations) is critical after all.  Latency of one dependent addition at a
   // reduction's occupancy: about 11 us (G1), 29 us (G2), measured on GB300.
+  // It takes the critical shapes only when it would outlast its budget twice over (by one time,
+  // SquareChain(2^15) and 2^16 proofs measured 1-4% slower: reductions near their budget are
+  // hidden well enough).  A critical reduction that ends while the host pool is otherwise idle
+  // (not one of a small proof's reductions, which end together and share the pool with the
+  // combine's products) has its host part sums priced as the pool runs them.  Interleaved on
+  // one GB300 against the fixed rule (only the last MSM critical): SquareChain(2^13) 2.12 ->
+  // 1.24 ms, 2^14 2.09 -> 1.68 ms, 2^16 3.75 -> 3.70 ms, 2^10 / 2^12 / 2^18 level.
   bool critical = plan.latency_critical;
-  if (!critical && plan.hidden_us > 0 && rsh.cost * (FW == 16 ? 29.0 : 11.0) > plan.hidden_us) {
+  if (!critical && plan.hidden_us > 0 && rsh.cost * (FW == 16 ? 29.0 : 11.0) > 2.0 * plan.hidden_us)
     critical = true;
-    rsh = reduce_shape<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, 256u);
-  }
+  const bool pooled = critical && plan.host_pool_free;
+  if (pooled) rsh = reduce_shape<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, 256u, true);
   // a reduction that ends a critical path may take the cooperative form (8 lanes per addition)
   if (critical && ctx.coop_reduce != 0) {
-    const ReduceShape csh = reduce_shape_coop<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count);
+    const ReduceShape csh = reduce_shape_coop<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, pooled);
     if (ctx.coop_reduce > 0 || csh.cost < rsh.cost) rsh = csh;
   }
   const uint32_t RT = rsh.RT, M = rsh.M, J = rsh.J;

@@ -26,6 +26,9 @@ struct MsmPlan {
   // on the accumulation stream, which it should finish under; a longer reduction by the latency
   // model is treated as critical (0 = no budget known: trust latency_critical)
   double hidden_us = 0;
+  // the host pool is otherwise idle when this reduction ends (not one of a small proof's
+  // reductions that end together), so its part sums are priced as the pool runs them
+  bool host_pool_free = false;
 };
 
 // Window table of a fixed point set: row w (w < W) holds 2^(o_w) P_i for all i (o_w the bit

@@ -499,6 +499,7 @@ void prove_resident(Ctx& ctx, PkDev& pk, const uint32_t* witness16, const uint32
     // others get the accumulation time queued after them (entries x about 0.3 ns for G1 and
     // 0.9 ns for G2 inside a proof), which the reduction should not outlast.
     p.latency_critical = overlap || j == 4;
+    p.host_pool_free = !overlap && !ctx.shared_gpu;
     // (Batch and server lanes keep the fixed rule: other proofs fill the GPU there.)
     p.hidden_us = 0;
     if (!ctx.shared_gpu)
