@@ -714,6 +714,42 @@ ReduceShape reduce_shape(uint32_t nb, int sets, size_t entries, uint32_t K, int 
   return best;
 }
 
+// A hidden reduction's shape by work instead of latency: the one with the fewest warp-additions
+// per bucket (the running sums, plus the scan, doublings and tree that a CTA of RT threads adds
+// on top, counted per warp as a warp issues them) whose latency by reduce_shape's model stays
+// within `max_cost` dependent additions; {0, 0, 0} when none does.
+template <class F>
+ReduceShape reduce_shape_work(uint32_t nb, int sets, size_t entries, uint32_t K, int sm_count, uint32_t max_rt,
+                              double max_cost) {
+  const double e = (double)entries / ((double)nb * sets);
+  const double per_bucket = 2.0 + e / K;
+  ReduceShape best{0, 0, 0, 1e300, false};
+  double best_work = 1e300;
+  for (uint32_t RT = 32; RT <= max_rt; RT <<= 1) {
+    for (uint32_t M = 1; M <= 16; M <<= 1) {
+      if ((uint64_t)RT * M > nb) continue;
+      const uint32_t J = nb / (RT * M);
+      int lrt = 0, lm = 0;
+      while ((1u << lrt) < RT) lrt++;
+      while ((1u << lm) < M) lm++;
+      const double slots = (double)sm_count * reduce_blocks_per_sm<F>(RT);
+      const double waves = std::ceil((double)J * sets / slots);
+      const double cost = waves * (M * per_bucket + 2.0 * lrt + lm) + host_parts_cost(J, sets, false);
+      if (cost > max_cost) continue;
+      const double warps = RT / 32.0;
+      double scan = 0, tree = 0;
+      for (uint32_t d = 1; d < RT; d <<= 1) scan += std::ceil((RT - d) / 32.0);
+      for (uint32_t d = RT >> 1; d >= 1; d >>= 1) tree += std::ceil(d / 32.0);
+      const double work = (warps * M * per_bucket + scan + warps * (lm + 1) + tree) / ((double)RT * M);
+      if (work < best_work - 1e-12) {
+        best_work = work;
+        best = {RT, M, J, cost, false};
+      }
+    }
+  }
+  return best;
+}
+
 #include "msm_coop.cuh"
 
 // The cooperative form's shape by the same model: RT groups (of 8 lanes) per CTA, each addition
@@ -922,8 +958,20 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   // one GB300 against the fixed rule (only the last MSM critical): SquareChain(2^13) 2.12 ->
   // 1.24 ms, 2^14 2.09 -> 1.68 ms, 2^16 3.75 -> 3.70 ms, 2^10 / 2^12 / 2^18 level.
   bool critical = plan.latency_critical;
-  if (!critical && plan.hidden_us > 0 && rsh.cost * (FW == 16 ? 29.0 : 11.0) > 2.0 * plan.hidden_us)
-    critical = true;
+  const double add_us = FW == 16 ? 29.0 : 11.0;
+  if (!critical && plan.hidden_us > 0 && rsh.cost * add_us > 2.0 * plan.hidden_us) critical = true;
+  // A hidden G1 reduction takes the shape with the least work per bucket (longer chains, fewer
+  // scan, doubling and tree additions per bucket) whose modelled latency stays within a quarter
+  // of its budget (the model underestimates a reduction running beside accumulations by 1.3-2x).
+  // Interleaved against the shortest-chain shapes on one GB300: SquareChain(2^16) 3.69 ->
+  // 3.46 ms, 2^17 6.14 -> 5.96 ms, 2^18 10.55 -> 10.48 ms, 2^14 and 2^20 level.  For G2 it
+  // measured level to 1% slower at 2^20 (the G2 reduction stretched 2.9 -> 5.1 ms and crowded
+  // the last accumulations), so G2 keeps the shortest chain.
+  if (!critical && plan.hidden_us > 0 && FW == 8) {
+    const ReduceShape wsh =
+        reduce_shape_work<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, 128u, 0.25 * plan.hidden_us / add_us);
+    if (wsh.RT) rsh = wsh;
+  }
   const bool pooled = critical && plan.host_pool_free;
   if (pooled) rsh = reduce_shape<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, 256u, true);
   // a reduction that ends a critical path may take the cooperative form (8 lanes per addition)
