@@ -523,7 +523,7 @@ def batched(ctx, args, flush, ext, imad_peak=None):
     plain(), batch(8)  # warm every lane and workspace
     ref, t_plain = timed(plain)
     lanes_best, t_best, got = None, None, None
-    for lanes in (4, 8, 12):
+    for lanes in BATCH_LANES:
         out, t = timed(lambda: batch(lanes))
         if t_best is None or t < t_best:
             lanes_best, t_best, got = lanes, t, out
@@ -553,7 +553,11 @@ def batched(ctx, args, flush, ext, imad_peak=None):
             "bit_exact_vs_plain": bool(exact), "roofline": roof}
 
 
+# lanes (concurrent provers) the batch is timed with (the best is reported)
+BATCH_LANES = (4, 8, 12)
 SERVE_KS = (12, 14, 16, 18, 20)
+SERVE_LANES = 8
+SERVE_HBM_BUDGET = 64 << 30
 SERVE_WEIGHTS = (0.3, 0.25, 0.2, 0.15, 0.1)
 SERVE_RATES = (10, 50, 100, 200, 500)
 
@@ -593,7 +597,7 @@ def single_proofs(ctx, key, path, reps=5):
             "proof_verified": bool(ok), "timing": "wall clock of bg_prove_resident, median of %d" % reps}
 
 
-def serving(ctx, args, lanes=8, seconds=1.5):
+def serving(ctx, args, lanes=None, seconds=1.5, budget=None):
     """The serving workload: Poisson arrivals of prove requests with K drawn from
     SERVE_KS, all five proving keys resident, continuous batching in the library's server;
     p50 / p99 latency (submit -> proof) and completed proofs/s per offered rate."""
@@ -616,7 +620,8 @@ def serving(ctx, args, lanes=8, seconds=1.5):
         paths[k] = path
         del f
     k20 = single_proofs(ctx, keys[SERVE_KS[-1]], paths[SERVE_KS[-1]])
-    budget = 64 << 30
+    lanes = lanes or SERVE_LANES
+    budget = budget or SERVE_HBM_BUDGET
     srv = bendg.Server(ctx, lanes=lanes, hbm_budget_bytes=budget)
     # warm every lane on the largest key
     for t in range(lanes):
