@@ -15,7 +15,7 @@ constexpr signed char kTuneSets[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
 // window tables of resident keys (one shared bucket set)
 constexpr signed char kTuneTables[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
     {9, 0, 11, 0, 13, 0, 15, 0, 17, 0, 19, 0, 0},
-    {10, 0, 11, 0, 14, 0, 15, 0, 17, 0, 17, 0, 0}};
+    {11, 0, 11, 0, 13, 0, 15, 0, 18, 0, 17, 0, 0}};
 // one bucket set per window inside a proof (one-shot proofs): the MSMs share the GPU with
 // each other's reductions and the QAP, which moves the best width from the standalone one
 constexpr signed char kTuneProofSets[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
