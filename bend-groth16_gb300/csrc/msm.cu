@@ -227,16 +227,56 @@ __global__ void __launch_bounds__(128) k_build_table(const uint32_t* __restrict_
 // repeated thousands of times) is joined beforehand by k_bucket_heavy: the thread that owns its
 // first piece lists it in heavy[1 + i] (heavy[0] counts, cleared before the accumulation).
 constexpr uint32_t kPieceLimit = 24;
+// G2's accumulation stages the next entry's point in shared memory (cp.async) instead of
+// registers, where a prefetched Fq2 point held 32 registers across the whole addition: 222
+// registers instead of 242, the G2 accumulation of a 2^18 MSM 2.96 -> 2.93 ms,
+// SquareChain(2^18) 9.88 -> 9.75-9.79 ms, 2^20 34.8 -> 34.4-34.5 ms.  The registers saved do
+// not buy more warps: capped at 200 (10 warps per SM in 64-thread CTAs, a few spills) or 216
+// (9 warps in 32-thread CTAs) the same kernel measured 3.14 / 3.12 ms.  G1 keeps its register
+// prefetch (126 registers, four 128-thread CTAs per SM either way).
+template <class F>
+constexpr bool kAccStaged = FieldWords<F>::value == 16;
 // CTA size of the accumulation
 template <class F>
 constexpr int kAccThreads = 128;
 
+// 16-byte asynchronous copy global -> shared (cached in L2 only), and the wait for a thread's
+// own copies
+BG_DEV void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+BG_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+BG_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// the affine point held in 16-byte chunks c[0 .. 2 FW / 4)
+BG_DEV Fq fp_of(const uint4& a, const uint4& b) {
+  Fq r;
+  r.v[0] = a.x; r.v[1] = a.y; r.v[2] = a.z; r.v[3] = a.w;
+  r.v[4] = b.x; r.v[5] = b.y; r.v[6] = b.z; r.v[7] = b.w;
+  return r;
+}
+template <class F>
+BG_DEV Affine<F> affine_of_chunks(const uint4* c, size_t stride) {
+  Affine<F> p;
+  if constexpr (FieldWords<F>::value == 16) {
+    p.x.c0 = fp_of(c[0], c[stride]);
+    p.x.c1 = fp_of(c[2 * stride], c[3 * stride]);
+    p.y.c0 = fp_of(c[4 * stride], c[5 * stride]);
+    p.y.c1 = fp_of(c[6 * stride], c[7 * stride]);
+  } else {
+    p.x = fp_of(c[0], c[stride]);
+    p.y = fp_of(c[2 * stride], c[3 * stride]);
+  }
+  return p;
+}
+
 template <class F>
 __global__ void __launch_bounds__(kAccThreads<F>) k_bucket_acc(const uint32_t* __restrict__ points,
-                                                    const uint32_t* __restrict__ offsets,
-                                                    const uint32_t* __restrict__ sorted, uint32_t nbuckets,
-                                                    uint32_t K, uint32_t* __restrict__ buckets,
-                                                    uint32_t* __restrict__ parts, uint32_t* __restrict__ heavy) {
+                                                               const uint32_t* __restrict__ offsets,
+                                                               const uint32_t* __restrict__ sorted, uint32_t nbuckets,
+                                                               uint32_t K, uint32_t* __restrict__ buckets,
+                                                               uint32_t* __restrict__ parts, uint32_t* __restrict__ heavy) {
   constexpr int FW = FieldWords<F>::value;
   constexpr int PW = 4 * FW;
   const uint32_t total = offsets[nbuckets];
@@ -259,20 +299,41 @@ __global__ void __launch_bounds__(kAccThreads<F>) k_bucket_acc(const uint32_t* _
   XYZZ<F> acc = xyzz_inf<F>();
   // The next entry's point is gathered before this entry's addition, so the gather's latency
   // hides behind the arithmetic (G1 accumulation 2^20 3.88 -> 3.82 ms; 126 registers, still
-  // four CTAs per SM).
+  // four CTAs per SM): into registers for G1, into one of two shared-memory slots for G2 (the
+  // slot read in this iteration is refilled two iterations later, after the addition that
+  // consumed it).
   // sorted == nullptr: the entries are the points themselves (the output of the pair rounds)
+  constexpr int CH = 2 * FW / 4;  // 16-byte chunks of an affine point
+  __shared__ uint4 stage[kAccStaged<F> ? 2 : 1][kAccStaged<F> ? CH : 1][kAccThreads<F>];
+  auto gather = [&](uint32_t c, int slot) {
+    const uint4* src = reinterpret_cast<const uint4*>(points + (size_t)(c & 0x7fffffffu) * 2 * FW);
+#pragma unroll
+    for (int j = 0; j < CH; j++) cp_async16(&stage[slot][j][threadIdx.x], src + j);
+    cp_async_commit();
+  };
   uint32_t code = sorted ? sorted[beg] : beg;
-  Affine<F> p = load_affine<F>(points + (size_t)(code & 0x7fffffffu) * 2 * FW);
+  Affine<F> p;
+  if constexpr (kAccStaged<F>) gather(code, 0);
+  else p = load_affine<F>(points + (size_t)(code & 0x7fffffffu) * 2 * FW);
+  int slot = 0;
   for (uint32_t e = beg; e < end; e++) {
     uint32_t code_n = 0;
     Affine<F> pn;
-    if (e + 1 < end) {
+    if constexpr (kAccStaged<F>) {
+      cp_async_wait_all();
+      p = affine_of_chunks<F>(&stage[slot][0][threadIdx.x], kAccThreads<F>);
+      if (e + 1 < end) {
+        code_n = sorted ? sorted[e + 1] : e + 1;
+        gather(code_n, slot ^ 1);
+      }
+      slot ^= 1;
+    } else if (e + 1 < end) {
       code_n = sorted ? sorted[e + 1] : e + 1;
       pn = load_affine<F>(points + (size_t)(code_n & 0x7fffffffu) * 2 * FW);
     }
     if (code >> 31) p = affine_neg(p);
     acc = xyzz_madd(acc, p);
-    p = pn;
+    if constexpr (!kAccStaged<F>) p = pn;
     code = code_n;
     if (e + 1 == bend || e + 1 == end) {
       if (bstart < beg || bend > end) {
