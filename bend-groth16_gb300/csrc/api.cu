@@ -84,6 +84,11 @@ int arg_error(bg_ctx* ctx, const char* fn, const char* condition) {
     if (bad) return arg_error((ctx), __func__, #bad);       \
   } while (0)
 
+// Device buffers handed to the _dev entry points are read and written in 16-byte vectors (and
+// gathered by 16-byte asynchronous copies): a pointer off that boundary is refused here rather
+// than left to fault on the device.  cudaMalloc returns 256-byte aligned memory.
+inline bool misaligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) != 0; }
+
 void require(bool ok, const char* msg) {
   if (!ok) throw Error(BG_E_ARG, msg);
 }
@@ -376,6 +381,7 @@ int bg_msm_g2(bg_ctx* ctx, const uint32_t* points16, const uint32_t* scalars16, 
 }
 
 int bg_msm_g1_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32) {
+  BG_ARG_CHECK(ctx, misaligned16(d_points) || misaligned16(d_scalars));
   BG_ARG_CHECK(ctx, !ctx || !out_aff32 || (n && (!d_points || !d_scalars)));
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
@@ -384,6 +390,7 @@ int bg_msm_g1_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scala
 }
 
 int bg_msm_g2_dev(bg_ctx* ctx, const uint32_t* d_points, const uint32_t* d_scalars, size_t n, uint32_t* out_aff32) {
+  BG_ARG_CHECK(ctx, misaligned16(d_points) || misaligned16(d_scalars));
   BG_ARG_CHECK(ctx, !ctx || !out_aff32 || (n && (!d_points || !d_scalars)));
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
@@ -427,6 +434,7 @@ int bg_ntt(bg_ctx* ctx, uint32_t* data16, uint32_t log2n, int mode) {
 }
 
 int bg_ntt_dev(bg_ctx* ctx, uint32_t* d_data, uint32_t log2n, int mode) {
+  BG_ARG_CHECK(ctx, misaligned16(d_data));
   BG_ARG_CHECK(ctx, !ctx || !d_data || log2n > 27 || mode < 0 || mode > 3);
   return guard(ctx, [&] {
     cudaSetDevice(ctx->c.device);
@@ -435,11 +443,13 @@ int bg_ntt_dev(bg_ctx* ctx, uint32_t* d_data, uint32_t log2n, int mode) {
 }
 
 int bg_repack_to_packed_dev(bg_ctx* ctx, const uint32_t* d_wire, uint32_t* d_packed, size_t n) {
+  BG_ARG_CHECK(ctx, misaligned16(d_wire) || misaligned16(d_packed));
   BG_ARG_CHECK(ctx, !ctx || (n && (!d_wire || !d_packed)));
   return guard(ctx, [&] { wire_to_packed(ctx->c.stream, d_wire, d_packed, n, ctx->c.d_status); });
 }
 
 int bg_repack_to_wire_dev(bg_ctx* ctx, const uint32_t* d_packed, uint32_t* d_wire, size_t n) {
+  BG_ARG_CHECK(ctx, misaligned16(d_wire) || misaligned16(d_packed));
   BG_ARG_CHECK(ctx, !ctx || (n && (!d_wire || !d_packed)));
   return guard(ctx, [&] { packed_to_wire(ctx->c.stream, d_packed, d_wire, n); });
 }

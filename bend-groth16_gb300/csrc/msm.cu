@@ -1379,6 +1379,12 @@ extern "C" int bg_msm_g1_noalloc(const uint32_t* d_points, const uint32_t* d_sca
     bg::set_noctx_error("bg_msm_g1_noalloc: invalid argument (a null pointer)");
     return BG_E_ARG;
   }
+  // points and scalars are read in 16-byte vectors: refuse a pointer off that boundary here
+  // rather than let the device fault on it
+  if ((reinterpret_cast<uintptr_t>(d_points) | reinterpret_cast<uintptr_t>(d_scalars)) & 15u) {
+    bg::set_noctx_error("bg_msm_g1_noalloc: invalid argument (a device pointer not 16-byte aligned)");
+    return BG_E_ARG;
+  }
   std::lock_guard<std::mutex> lock(bg::g_noalloc_mu);
   try {
     bg::msm_g1_noalloc(d_points, d_scalars, n, static_cast<cudaStream_t>(stream), out_aff32);

@@ -11,7 +11,8 @@
  * form with R = 2^256 except MSM scalars, which are canonical (bend2/src/msm.bend:3-5).
  * G1 affine = x, y (32 words); G2 affine = x.c0, x.c1, y.c0, y.c1 (64 words); the point at
  * infinity is all-zero words.  Functions whose names end in _dev take device pointers in the
- * packed layout (8 x u32 limbs per element, same Montgomery convention).
+ * packed layout (8 x u32 limbs per element, same Montgomery convention); those pointers (and
+ * bg_msm_g1_noalloc's) must be 16-byte aligned, as cudaMalloc's are (BG_E_ARG otherwise).
  *
  * Errors: every entry point returns 0 (BG_OK) or a BG_E_* status and never aborts; the
  * reference has no error channel on this path (an OOM ends the Bend process,

@@ -52,6 +52,33 @@ def test_argument_errors_carry_a_message(built_lib):
     assert L.bg_last_error(None).decode().startswith("bg_proof_format: invalid argument")
 
 
+def test_misaligned_device_pointers_are_refused(built_lib):
+    """the _dev entry points and bg_msm_g1_noalloc read and write device buffers in 16-byte
+    vectors: a pointer off that boundary is refused on the host, before any device work (the
+    pointer values here are never dereferenced, so no GPU is needed)"""
+    import bendg
+    L = bendg.lib()
+    out = (ctypes.c_uint32 * 48)()
+    bad, good = 0x10004, 0x10000
+    cases = [
+        ("bg_msm_g1_dev", lambda: L.bg_msm_g1_dev(None, bad, good, 4, out)),
+        ("bg_msm_g1_dev", lambda: L.bg_msm_g1_dev(None, good, bad, 4, out)),
+        ("bg_msm_g2_dev", lambda: L.bg_msm_g2_dev(None, bad, good, 4, out)),
+        ("bg_ntt_dev", lambda: L.bg_ntt_dev(None, bad, 10, 0)),
+        ("bg_repack_to_packed_dev", lambda: L.bg_repack_to_packed_dev(None, good, bad, 4)),
+        ("bg_repack_to_wire_dev", lambda: L.bg_repack_to_wire_dev(None, bad, good, 4)),
+    ]
+    for name, call in cases:
+        assert call() == bendg.BG_E_ARG, name
+        msg = L.bg_last_error(None).decode()
+        assert msg.startswith(name + ": invalid argument") and "misaligned16" in msg, msg
+    assert L.bg_msm_g1_noalloc(good, bad, 4, None, out) == bendg.BG_E_ARG
+    assert "16-byte aligned" in L.bg_last_error(None).decode()
+    # aligned pointers pass the alignment check and stop at the missing context instead
+    assert L.bg_msm_g1_dev(None, good, good, 4, out) == bendg.BG_E_ARG
+    assert "!ctx" in L.bg_last_error(None).decode()
+
+
 def test_no_device_fails_loudly(built_lib):
     """without a usable GPU, creating a context fails with BG_E_DEVICE and the CUDA reason:
     there is no CPU fallback behind the C ABI"""
