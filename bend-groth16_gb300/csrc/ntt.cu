@@ -28,8 +28,7 @@ namespace bg {
 
 constexpr int kNttThreads = 256;
 constexpr int kNttTile = 1024;   // elements per CTA tile (32 KiB of shared memory)
-constexpr int kContigMax = 10;   // stages in the contiguous pass
-constexpr int kStridedMax = 10;  // stages in a strided pass (each element is a whole 32-byte sector)
+constexpr int kContigMax = 10;   // stages in one pass, contiguous or strided (a 1024-element tile)
 
 enum ScaleMode { SC_NONE = 0, SC_NATURAL = 1, SC_BITREV = 2, SC_CONST = 3 };
 
