@@ -1004,7 +1004,8 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
 
   // A reduction hidden under a later accumulation keeps its CTAs at 128 threads: a 256-thread
   // CTA of ~210 registers leaves no room for an accumulation CTA on its SM for its whole
-  // (latency-bound) life (K = 18 proof: caps 64 / 128 / 256 measured 11.0 / 10.8 / 10.8 ms).
+  // (latency-bound) life (K = 18 proof: caps 64 / 128 / 256 measured 11.0 / 10.8 / 10.8 ms
+  // with the reductions' streams first, 10.12 / 9.87 / 9.94 ms with the accumulations first).
   ReduceShape rsh =
       reduce_shape<F>(so.nb, so.sets, acc_entries, bs.K, ctx.sm_count, plan.latency_critical ? 256u : 128u);
   // A reduction meant to run under later accumulations that the latency model says outlasts
@@ -1013,7 +1014,7 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   // reduction's occupancy: about 11 us (G1), 29 us (G2), measured on GB300.
   // It takes the critical shapes only when it would outlast its budget twice over (by one time,
   // SquareChain(2^15) and 2^16 proofs measured 1-4% slower: reductions near their budget are
-  // hidden well enough).  A critical reduction that ends while the host pool is otherwise idle
+  // hidden well enough; by four times, 2^14 measured 1.59 -> 1.95 ms).  A critical reduction that ends while the host pool is otherwise idle
   // (not one of a small proof's reductions, which end together and share the pool with the
   // combine's products) has its host part sums priced as the pool runs them.  Interleaved on
   // one GB300 against the fixed rule (only the last MSM critical): SquareChain(2^13) 2.12 ->
@@ -1025,7 +1026,9 @@ void msm_accumulate(Ctx& ctx, cudaStream_t st, const std::string& tag, const uin
   // scan, doubling and tree additions per bucket) whose modelled latency stays within a quarter
   // of its budget (the model underestimates a reduction running beside accumulations by 1.3-2x).
   // Interleaved against the shortest-chain shapes on one GB300: SquareChain(2^16) 3.69 ->
-  // 3.46 ms, 2^17 6.14 -> 5.96 ms, 2^18 10.55 -> 10.48 ms, 2^14 and 2^20 level.  For G2 it
+  // 3.46 ms, 2^17 6.14 -> 5.96 ms, 2^18 10.55 -> 10.48 ms, 2^14 and 2^20 level; with the
+  // accumulations first, half or all of the budget instead of a quarter measured level to 6%
+  // slower (2^16 3.46 -> 3.51 / 3.69 ms).  For G2 it
   // measured level to 1% slower at 2^20 (the G2 reduction stretched 2.9 -> 5.1 ms and crowded
   // the last accumulations), so G2 keeps the shortest chain.
   if (!critical && plan.hidden_us > 0 && FW == 8) {
