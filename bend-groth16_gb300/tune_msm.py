@@ -42,6 +42,15 @@ def median_ms(fn, reps):
     return statistics.median(out)
 
 
+def same_result(seen, key, result):
+    """a width changes how a result is computed, never what it is: the first result for `key`
+    is kept, and any later width that gives another one stops the tuning"""
+    if key not in seen:
+        seen[key] = result
+    elif seen[key] != result:
+        raise RuntimeError("tune_msm: %s gave a different result at another window width" % (key,))
+
+
 def search(measure, lo, hi, c_min, c_max):
     """times of c in [lo, hi] (clamped to [c_min, c_max]), the range widened one step at a time
     while the fastest width sits on an edge of it"""
@@ -64,6 +73,7 @@ def tune_sets(ctx, torch, pts_g1, pts_g2, log2s_g1, log2s_g2, reps, log):
     dev = torch.device("cuda")
     rng = np.random.default_rng(12345)
     best = {0: {}, 1: {}}
+    seen = {}
     for curve, log2s, pts in ((bendg.CURVE_G1, log2s_g1, pts_g1), (bendg.CURVE_G2, log2s_g2, pts_g2)):
         pw = 16 if curve == bendg.CURVE_G1 else 32
         for lg in log2s:
@@ -78,6 +88,7 @@ def tune_sets(ctx, torch, pts_g1, pts_g2, log2s_g1, log2s_g2, reps, log):
 
             def measure(c):
                 ctx.window_override(0, curve, c)
+                same_result(seen, ("sets", curve, lg), f(p.data_ptr(), sc.data_ptr(), n).tobytes())
                 return median_ms(lambda: f(p.data_ptr(), sc.data_ptr(), n), reps)
             times = search(measure, rule - 2, rule + 2, 3, 20)
             ctx.window_override(0, curve, 0)
@@ -91,6 +102,7 @@ def tune_sets(ctx, torch, pts_g1, pts_g2, log2s_g1, log2s_g2, reps, log):
 def tune_tables(ctx, ks, data_root, reps, log):
     """layout 1: resident-key proofs with one curve's table width forced"""
     best = {0: {}, 1: {}}
+    seen = {}
     for k in ks:
         path = os.path.join(data_root, "sq%d" % k)
         if not os.path.exists(os.path.join(path, "vk.bin")):
@@ -107,6 +119,7 @@ def tune_tables(ctx, ks, data_root, reps, log):
                 for cv in (0, 1):
                     ctx.window_override(1, cv, forced[cv] if cv != curve else c)
                 key = ctx.pk_upload(files)
+                same_result(seen, ("table", k), ctx.proof_text(key.prove(w, rs)[0]))
                 t = median_ms(lambda: key.prove(w, rs), reps)
                 key.release()
                 return t
@@ -140,6 +153,7 @@ def tune_proof_sets(ctx, ks, data_root, reps, log):
     curve's width forced; every G1 MSM of a SquareChain(2^K) proof has floor(log2 n) = K, and so
     does the G2 one"""
     best = {0: {}, 1: {}}
+    seen = {}
     for k in ks:
         path = os.path.join(data_root, "sq%d" % k)
         if not os.path.exists(os.path.join(path, "vk.bin")):
@@ -152,6 +166,7 @@ def tune_proof_sets(ctx, ks, data_root, reps, log):
             def measure(c):
                 for cv in (0, 1):
                     ctx.window_override(0, cv, forced[cv] if cv != curve else c)
+                same_result(seen, ("proof", k), ctx.proof_text(ctx.prove_host(files)[0]))
                 return median_ms(lambda: ctx.prove_host(files), reps)
             times = search(measure, rule - 2, rule + 2, 3, 20)
             c_best = min(times, key=times.get)

@@ -3,6 +3,8 @@ widens its range while the fastest width sits on an edge, and the header it writ
 library compiles in.  No GPU: the measurements are a fake cost curve."""
 import re
 
+import pytest
+
 import tune_msm
 
 
@@ -28,6 +30,17 @@ def test_search_widens_past_the_upper_edge_and_clamps():
 def test_search_interior_optimum_measures_only_the_range():
     times = tune_msm.search(lambda c: (c - 12) ** 2, 10, 14, 3, 20)
     assert sorted(times) == [10, 11, 12, 13, 14]
+
+
+def test_a_width_that_changes_the_result_stops_the_tuning():
+    """every width must give the same MSM result or proof; the tuner keeps the first and stops
+    at the first width that differs, so no such width can reach the committed header"""
+    seen = {}
+    tune_msm.same_result(seen, ("table", 18), "A 0x1")
+    tune_msm.same_result(seen, ("table", 18), "A 0x1")
+    tune_msm.same_result(seen, ("table", 20), "A 0x2")
+    with pytest.raises(RuntimeError):
+        tune_msm.same_result(seen, ("table", 18), "A 0x3")
 
 
 def test_header_text_rows():
