@@ -14,12 +14,12 @@ constexpr signed char kTuneSets[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
     {8, 9, 9, 9, 9, 10, 11, 12, 15, 15, 15, 0, 0}};
 // window tables of resident keys (one shared bucket set)
 constexpr signed char kTuneTables[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
-    {9, 0, 11, 0, 13, 0, 15, 0, 17, 0, 17, 0, 0},
+    {9, 0, 11, 0, 14, 0, 15, 0, 17, 0, 17, 0, 0},
     {11, 0, 11, 0, 13, 0, 15, 0, 18, 0, 17, 0, 0}};
 // one bucket set per window inside a proof (one-shot proofs): the MSMs share the GPU with
 // each other's reductions and the QAP, which moves the best width from the standalone one
 constexpr signed char kTuneProofSets[2][kTuneMaxLog2 - kTuneMinLog2 + 1] = {
-    {10, 0, 11, 0, 9, 0, 12, 0, 13, 0, 15, 0, 0},
+    {10, 0, 11, 0, 10, 0, 12, 0, 13, 0, 15, 0, 0},
     {8, 0, 9, 0, 9, 0, 12, 0, 14, 0, 15, 0, 0}};
 
 }  // namespace bg
