@@ -304,12 +304,15 @@ __global__ void __launch_bounds__(kAccThreads<F>) k_bucket_acc(const uint32_t* _
   // consumed it).
   // sorted == nullptr: the entries are the points themselves (the output of the pair rounds)
   constexpr int CH = 2 * FW / 4;  // 16-byte chunks of an affine point
-  __shared__ uint4 stage[kAccStaged<F> ? 2 : 1][kAccStaged<F> ? CH : 1][kAccThreads<F>];
+  constexpr int kSlots = kAccStaged<F> ? 2 : 1, kChunks = kAccStaged<F> ? CH : 1;
+  __shared__ uint4 stage[kSlots][kChunks][kAccThreads<F>];
   auto gather = [&](uint32_t c, int slot) {
-    const uint4* src = reinterpret_cast<const uint4*>(points + (size_t)(c & 0x7fffffffu) * 2 * FW);
+    if constexpr (kAccStaged<F>) {
+      const uint4* src = reinterpret_cast<const uint4*>(points + (size_t)(c & 0x7fffffffu) * 2 * FW);
 #pragma unroll
-    for (int j = 0; j < CH; j++) cp_async16(&stage[slot][j][threadIdx.x], src + j);
-    cp_async_commit();
+      for (int j = 0; j < CH; j++) cp_async16(&stage[slot][j][threadIdx.x], src + j);
+      cp_async_commit();
+    }
   };
   uint32_t code = sorted ? sorted[beg] : beg;
   Affine<F> p;
